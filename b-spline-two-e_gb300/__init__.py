@@ -1,0 +1,288 @@
+"""GB300 two-electron matrix elements for B-spline bases (host-side mirror).
+
+Python mirror of the interface that basis_setup uses in edvinolo/b-spline-two-e
+(src/apps/main_basis_setup.f90:75-118) on top of the C-ABI CUDA library
+libbs2e.so (include/bs2e.h).  The compute path is the CUDA library only: if
+libbs2e.so cannot be loaded every call raises; nothing here falls back to a CPU
+implementation.
+
+Typical use, mirroring main_basis_setup.f90:
+    h = Bs2e(knots, k, k_GL, max_k)          # splines%init + r_k/r_m_k/r_d_k%init
+    h.slater()                               # setup_Slater_integrals
+    h.rk()                                   # compute_R_k_map
+    h.one_body(Z, n_l, ...)                  # setup_S / setup_H_one_particle
+    for sym in symmetries(...):              # bas%init
+        H, S = h.block(configs, sym.L, full)  # count_nnz + construct_block_tensor
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import grids, basis  # noqa: F401  (re-exported helpers)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libbs2e.so")
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+_STATUS = {
+    0: "BS2E_OK", 1: "BS2E_ERR_ARG", 2: "BS2E_ERR_NOMEM", 3: "BS2E_ERR_CUDA",
+    4: "BS2E_ERR_COUNT", 5: "BS2E_ERR_TIMEOUT", 6: "BS2E_ERR_STATE", 7: "BS2E_ERR_NODEV",
+    8: "BS2E_ERR_ORDER",
+}
+
+# Every symbol include/bs2e.h declares (checked by the CPU tests).
+EXPORTS = [
+    "bs2e_default_opts", "bs2e_create", "bs2e_destroy", "bs2e_last_error", "bs2e_sizes",
+    "bs2e_slater", "bs2e_get_primitives", "bs2e_rk", "bs2e_rk_get", "bs2e_rk_get_batch",
+    "bs2e_set_one_body", "bs2e_one_body", "bs2e_block_count", "bs2e_block_fill",
+    "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_configs", "bs2e_ang_k_LS",
+    "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
+]
+
+
+class Bs2eError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__("%s: %s" % (_STATUS.get(status, str(status)), msg))
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int64), ("device", ctypes.c_int64),
+                ("reserved", ctypes.c_int64 * 6)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libbs2e.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise Bs2eError(3, "libbs2e.so not built at %s (run build.py)" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    i64, p, dbl = ctypes.c_int64, ctypes.c_void_p, ctypes.c_double
+    st = ctypes.c_int32
+    sig = {
+        "bs2e_default_opts": (None, [p]),
+        "bs2e_create": (st, [p, i64, i64, i64, i64, p, p]),
+        "bs2e_destroy": (st, [p]),
+        "bs2e_last_error": (st, [p, p, i64]),
+        "bs2e_sizes": (st, [p, p, p, p, p]),
+        "bs2e_slater": (st, [p]),
+        "bs2e_get_primitives": (st, [p, p, p, p, p, p]),
+        "bs2e_rk": (st, [p, i64, i64]),
+        "bs2e_rk_get": (st, [p, p, p]),
+        "bs2e_rk_get_batch": (st, [p, i64, p, p]),
+        "bs2e_set_one_body": (st, [p, p, i64, p]),
+        "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
+        "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
+        "bs2e_block_fill": (st, [p, p, i64, i64, i64, p, i64, p, p, p, p, p, p, p]),
+        "bs2e_block_count_ex": (st, [p, p, i64, i64, i64, i64, p, p]),
+        "bs2e_block_fill_ex": (st, [p, p, i64, i64, i64, i64, p, p, p, p, p, p, i64]),
+        "bs2e_configs": (st, [i64, i64, i64, i64, i64, i64, i64, i64, i64, p, p]),
+        "bs2e_ang_k_LS": (dbl, [i64, i64, i64, i64, i64, i64]),
+        "bs2e_three_j": (dbl, [i64, i64, i64, i64, i64, i64]),
+        "bs2e_six_j": (dbl, [i64, i64, i64, i64, i64, i64]),
+        "bs2e_stream": (st, [p, p]),
+        "bs2e_launch_count": (st, [p, p]),
+        "bs2e_synchronize": (st, [p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+CONFIG_DTYPE = np.dtype([("n1", "<i8"), ("n2", "<i8"), ("l1", "<i8"), ("l2", "<i8"),
+                         ("eqv", "<i8")])
+
+
+def as_configs(cf):
+    """Configuration list as a contiguous int64 record array (n1, n2, l1, l2, eqv)."""
+    a = np.asarray(cf)
+    if a.dtype == CONFIG_DTYPE:
+        return np.ascontiguousarray(a)
+    a = np.ascontiguousarray(a, dtype=np.int64).reshape(-1, 5)
+    return a.view(CONFIG_DTYPE).reshape(-1)
+
+
+def configs(L, parity_odd, max_l_1p, n_b, k, max_n_b=None, n_all_l=None, l2_max=None, spin=0):
+    """count_configs (src/tools/orbital_tools.f90:119-216) through the library."""
+    L_ = lib()
+    max_n_b = n_b if max_n_b is None else max_n_b
+    n_all_l = n_b if n_all_l is None else n_all_l
+    l2_max = max_l_1p if l2_max is None else l2_max
+    n = ctypes.c_int64()
+    args = [L, int(parity_odd), max_l_1p, n_b, k, max_n_b, n_all_l, l2_max, spin]
+    _check(None, L_.bs2e_configs(*args, None, ctypes.byref(n)))
+    out = np.zeros(n.value, dtype=CONFIG_DTYPE)
+    _check(None, L_.bs2e_configs(*args, _ptr(out), ctypes.byref(n)))
+    return out
+
+
+def ang_k_LS(k, la, lb, lc, ld, L):
+    return lib().bs2e_ang_k_LS(k, la, lb, lc, ld, L)
+
+
+def three_j(ja, jb, jc, ma, mb, mc):
+    return lib().bs2e_three_j(ja, jb, jc, ma, mb, mc)
+
+
+def six_j(ja, jb, jc, jd, je, jf):
+    return lib().bs2e_six_j(ja, jb, jc, jd, je, jf)
+
+
+def _check(h, status):
+    if status != 0:
+        msg = ""
+        if h is not None:
+            buf = ctypes.create_string_buffer(1024)
+            lib().bs2e_last_error(h, buf, 1024)
+            msg = buf.value.decode(errors="replace")
+        raise Bs2eError(status, msg)
+
+
+class Bs2e:
+    """One B-spline basis on one GPU (wraps a bs2e_handle)."""
+
+    def __init__(self, knots, k, k_GL, max_k, precision=PREC_FP64, device=0):
+        L_ = lib()
+        self.knots = np.ascontiguousarray(knots, dtype=np.float64)
+        self.k, self.k_GL, self.max_k = int(k), int(k_GL), int(max_k)
+        self.K1 = self.max_k + 1
+        opts = _Opts()
+        L_.bs2e_default_opts(ctypes.byref(opts))
+        opts.precision = int(precision)
+        opts.device = int(device)
+        h = ctypes.c_void_p()
+        st = L_.bs2e_create(_ptr(self.knots), self.knots.size, self.k, self.k_GL, self.max_k,
+                            ctypes.byref(opts), ctypes.byref(h))
+        if st != 0:
+            raise Bs2eError(st, "bs2e_create failed")
+        self._h = h
+        nb, niv, n4, n6 = (ctypes.c_int64() for _ in range(4))
+        _check(h, L_.bs2e_sizes(h, *(ctypes.byref(x) for x in (nb, niv, n4, n6))))
+        self.n_b, self.n_iv, self.nnz4, self.nnz6 = nb.value, niv.value, n4.value, n6.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bs2e_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- radial stage --------------------------------------------------------
+    def slater(self):
+        _check(self._h, lib().bs2e_slater(self._h))
+
+    def primitives(self, with_diag=True):
+        """r_k, r_m_k (nnz4 x K1), idx4 (nnz4 x 3), r_d_k (nnz6 x K1), idx6 (nnz6 x 5)."""
+        rk = np.zeros((self.nnz4, self.K1), order="F")
+        rmk = np.zeros((self.nnz4, self.K1), order="F")
+        i4 = np.zeros((self.nnz4, 3), dtype=np.int64)
+        rdk = i6 = None
+        if with_diag:
+            rdk = np.zeros((self.nnz6, self.K1), order="F")
+            i6 = np.zeros((self.nnz6, 5), dtype=np.int64)
+        _check(self._h, lib().bs2e_get_primitives(self._h, _ptr(rk), _ptr(rmk), _ptr(i4),
+                                                  _ptr(rdk), _ptr(i6)))
+        return dict(r_k=rk, r_m_k=rmk, idx4=i4, r_d_k=rdk, idx6=i6)
+
+    def rk(self, k_first=0, k_count=None):
+        k_count = self.K1 - k_first if k_count is None else k_count
+        _check(self._h, lib().bs2e_rk(self._h, k_first, k_count))
+
+    def rk_get(self, keys):
+        """R^k values (n x K1) of 1-based keys [a,b,c,d] (n x 4)."""
+        keys = np.ascontiguousarray(keys, dtype=np.int64).reshape(-1, 4)
+        vals = np.zeros((keys.shape[0], self.K1))
+        _check(self._h, lib().bs2e_rk_get_batch(self._h, keys.shape[0], _ptr(keys), _ptr(vals)))
+        return vals
+
+    # -- one-body matrices ---------------------------------------------------
+    def one_body(self, Z, n_l, cap_order=2, cap_r0=10.0, cap_eta=1e-3 + 0j, copy_out=True):
+        H = S = None
+        if copy_out:
+            H = np.zeros((self.n_b, self.n_b, n_l), dtype=np.complex128, order="F")
+            S = np.zeros((self.n_b, self.n_b), dtype=np.complex128, order="F")
+        eta = complex(cap_eta)
+        _check(self._h, lib().bs2e_one_body(self._h, int(Z), int(n_l), int(cap_order),
+                                            float(cap_r0), eta.real, eta.imag, _ptr(H), _ptr(S)))
+        return H, S
+
+    def set_one_body(self, H1p, S):
+        H1p = np.asfortranarray(H1p, dtype=np.complex128)
+        S = np.asfortranarray(S, dtype=np.complex128)
+        n_l = H1p.shape[2] if H1p.ndim == 3 else 1
+        _check(self._h, lib().bs2e_set_one_body(self._h, _ptr(H1p), n_l, _ptr(S)))
+
+    # -- symmetry blocks -------------------------------------------------------
+    def block_count(self, cf, L, full=True, spin=0):
+        cf = as_configs(cf)
+        nh, ns = ctypes.c_int64(), ctypes.c_int64()
+        _check(self._h, lib().bs2e_block_count_ex(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                  int(bool(full)), ctypes.byref(nh),
+                                                  ctypes.byref(ns)))
+        return nh.value, ns.value
+
+    def block(self, cf, L, full=True, spin=0):
+        """count + fill into host arrays; returns (H, S) dicts of 1-based CSR arrays."""
+        cf = as_configs(cf)
+        nh, ns = self.block_count(cf, L, full, spin)
+        n = cf.size
+        H = dict(shape=(n, n), nnz=nh, index_ptr=np.zeros(n + 1, np.int64),
+                 indices=np.zeros(nh, np.int64), data=np.zeros(nh, np.complex128))
+        S = dict(shape=(n, n), nnz=ns, index_ptr=np.zeros(n + 1, np.int64),
+                 indices=np.zeros(ns, np.int64), data=np.zeros(ns, np.complex128))
+        self.block_fill_into(cf, L, full, spin, H, S, on_device=False)
+        return H, S
+
+    def block_fill_into(self, cf, L, full, spin, H, S, on_device=False):
+        """Fills caller-provided arrays: numpy (host) or, with on_device, integer
+        device addresses in the dicts' 'index_ptr', 'indices', 'data' entries."""
+        cf = as_configs(cf)
+        if on_device:
+            args = [ctypes.c_void_p(int(H[x])) for x in ("index_ptr", "indices", "data")]
+            args += [ctypes.c_void_p(int(S[x])) for x in ("index_ptr", "indices", "data")]
+        else:
+            args = [_ptr(H[x]) for x in ("index_ptr", "indices", "data")]
+            args += [_ptr(S[x]) for x in ("index_ptr", "indices", "data")]
+        _check(self._h, lib().bs2e_block_fill_ex(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                 int(bool(full)), *args, int(bool(on_device))))
+
+    # -- plumbing ------------------------------------------------------------
+    @property
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(self._h, lib().bs2e_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    @property
+    def launch_count(self):
+        c = ctypes.c_int64()
+        _check(self._h, lib().bs2e_launch_count(self._h, ctypes.byref(c)))
+        return c.value
+
+    def synchronize(self):
+        _check(self._h, lib().bs2e_synchronize(self._h))

@@ -1,0 +1,37 @@
+"""Symmetry blocks of the two-electron basis (src/tools/orbital_tools.f90:245-343).
+
+symmetries() lists (L, M, parity) in the order init_basis creates them; the
+configuration list of each block comes from the library (bs2e_configs, a
+restatement of count_configs).  spin = 1 adds the triplet blocks, which the
+reference does not build.
+"""
+
+
+def count_terms(max_L, z_pol, two_el=True):
+    """count_terms (orbital_tools.f90:245-261)."""
+    if z_pol:
+        return max_L + 1
+    if two_el:
+        return (max_L + 1) ** 2
+    return max_L + 1 + max_L * (max_L + 1) // 2
+
+
+def symmetries(max_L, z_pol=True, two_el=True):
+    """(L, M, parity_odd) of every block in init_basis order (orbital_tools.f90:285-342)."""
+    out = [(0, 0, 0)]
+    if z_pol:
+        for L in range(1, max_L + 1):
+            out.append((L, 0, L % 2))
+    else:
+        for L in range(1, max_L + 1):
+            if two_el:
+                for p in (0, 1):
+                    for M in range(-L, L + 1):
+                        if abs(M % 2) != p:
+                            continue
+                        out.append((L, M, p))
+            else:
+                for M in range(-L, L + 1, 2):
+                    out.append((L, M, L % 2))
+    assert len(out) == count_terms(max_L, z_pol, two_el)
+    return out

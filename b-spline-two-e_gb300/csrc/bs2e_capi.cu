@@ -1,0 +1,643 @@
+// bs2e_capi.cu -- the extern "C" entry points declared in include/bs2e.h.
+//
+// Every entry point locks the handle, makes the handle's device current and
+// runs its kernels on the handle's stream.  Kernels are launched only through
+// the launchers of bs2e_radial.cu / bs2e_assembly.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bs2e_internal.h"
+
+namespace bs2e {
+size_t moments_smem(const Radial &g);
+size_t fill_smem(const Radial &g);
+uint64_t plan_signature(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
+                        int64_t full);
+}  // namespace bs2e
+
+using namespace bs2e;
+
+namespace {
+
+struct Guard {
+    bs2e_handle *h;
+    std::lock_guard<std::mutex> lk;
+    explicit Guard(bs2e_handle *hh) : h(hh), lk(hh->mu) { cudaSetDevice(hh->device); }
+};
+
+bs2e_status fail(bs2e_handle *h, bs2e_status st, const std::string &msg) {
+    if (h) h->err = msg;
+    return st;
+}
+
+#define CU(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA,  \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+    } while (0)
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+template <class T>
+void dfree(T *&p) {
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+// Waits for the stream and turns a set device error word into BS2E_ERR_TIMEOUT.
+bs2e_status sync_check(bs2e_handle *h, const char *what) {
+    CU(cudaStreamSynchronize(h->stream));
+    CU(cudaGetLastError());
+    int e = 0;
+    CU(cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        cudaMemset(h->d_err, 0, sizeof(int));
+        return fail(h, BS2E_ERR_TIMEOUT, std::string(what) + ": a bounded device wait expired");
+    }
+    return BS2E_OK;
+}
+
+// Number of basis splines (0-based b in [0,N)) non-zero on interval iv.
+int splines_on(const Radial &g, int iv) {
+    int lo = std::max(iv - 1, 0), hi = std::min(iv + g.k - 2, g.N - 1);
+    return hi >= lo ? hi - lo + 1 : 0;
+}
+
+void free_block(DevBlock &b) {
+    dfree(b.rows);
+    dfree(b.seg);
+    dfree(b.pairs);
+    dfree(b.pair_k);
+    dfree(b.pair_a);
+    dfree(b.pair_af);
+    dfree(b.tile_ab);
+    dfree(b.tile_ptr);
+    dfree(b.tile_rows);
+    dfree(b.cntH);
+    dfree(b.cntS);
+    dfree(b.scan_tmp);
+    b.n_tiles = 0;
+    b.nnzH = b.nnzS = -1;
+    b.sig = 0;
+}
+
+template <class T>
+bs2e_status upload(bs2e_handle *h, T **dst, const std::vector<T> &src) {
+    CU(dalloc(dst, src.size()));
+    if (!src.empty())
+        CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice,
+                           h->stream));
+    return BS2E_OK;
+}
+
+#define TRY(x)                              \
+    do {                                    \
+        bs2e_status s_ = (x);               \
+        if (s_ != BS2E_OK) return s_;       \
+    } while (0)
+
+// Builds, uploads and counts one block unless it is the cached one.
+bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_config, int64_t L,
+                           int64_t spin, int64_t full) {
+    if (!cf && n_config > 0) return fail(h, BS2E_ERR_ARG, "configs is NULL");
+    if (L < 0 || (spin != 0 && spin != 1) || (full != 0 && full != 1))
+        return fail(h, BS2E_ERR_ARG, "L, spin or full out of range");
+    uint64_t sig = plan_signature(cf, n_config, L, spin, full);
+    if (h->blk.sig == sig && h->blk.nnzH >= 0 && h->plan.n_config == n_config) return BS2E_OK;
+    free_block(h->blk);
+    std::string err;
+    bs2e_status st = build_plan(cf, n_config, L, spin, full, h->g, h->plan, err);
+    if (st != BS2E_OK) return fail(h, st, err);
+    BlockPlan &P = h->plan;
+    DevBlock &B = h->blk;
+    for (int c = 0; c < P.n_ch; ++c)
+        if (P.ch_l1[c] > 255 || P.ch_l2[c] > 255) return fail(h, BS2E_ERR_ARG, "l above 255");
+    std::vector<int4> rows((size_t)n_config);
+    for (int64_t i = 0; i < n_config; ++i) {
+        int c = P.row_ch[i];
+        rows[i] = make_int4(P.row_n1[i], P.row_n2[i], c, (P.ch_l1[c] << 8) | P.ch_l2[c]);
+    }
+    std::vector<int> seg;
+    seg.reserve(P.seg_base.size() * 3);
+    seg.insert(seg.end(), P.seg_base.begin(), P.seg_base.end());
+    seg.insert(seg.end(), P.seg_lo.begin(), P.seg_lo.end());
+    seg.insert(seg.end(), P.seg_hi.begin(), P.seg_hi.end());
+    std::vector<int> tab(P.tile_a.size() * 2);
+    for (size_t t = 0; t < P.tile_a.size(); ++t) {
+        tab[2 * t] = P.tile_a[t];
+        tab[2 * t + 1] = P.tile_b[t];
+    }
+    TRY(upload(h, &B.rows, rows));
+    TRY(upload(h, &B.seg, seg));
+    TRY(upload(h, &B.pairs, P.pairs));
+    TRY(upload(h, &B.pair_k, P.pair_k));
+    TRY(upload(h, &B.pair_a, P.pair_a));
+    TRY(upload(h, &B.pair_af, P.pair_af));
+    TRY(upload(h, &B.tile_ab, tab));
+    TRY(upload(h, &B.tile_ptr, P.tile_ptr));
+    TRY(upload(h, &B.tile_rows, P.tile_rows));
+    B.n_tiles = (int64_t)P.tile_a.size();
+    CU(dalloc(&B.cntH, (size_t)n_config));
+    CU(dalloc(&B.cntS, (size_t)n_config));
+    int64_t nparts = (n_config + 4095) / 4096 + 2;
+    CU(dalloc(&B.scan_tmp, (size_t)(nparts + 4)));
+    launch_block_count(h);
+    // totals of the construct predicate, and the count_nnz predicate in scan_tmp[0..1]
+    std::vector<int64_t> ch((size_t)n_config), cs((size_t)n_config);
+    unsigned long long ref[2] = {0, 0};
+    if (n_config > 0) {
+        CU(cudaMemcpyAsync(ch.data(), B.cntH, sizeof(int64_t) * n_config, cudaMemcpyDeviceToHost,
+                           h->stream));
+        CU(cudaMemcpyAsync(cs.data(), B.cntS, sizeof(int64_t) * n_config, cudaMemcpyDeviceToHost,
+                           h->stream));
+    }
+    CU(cudaMemcpyAsync(ref, B.scan_tmp, sizeof(ref), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "block count"));
+    int64_t th = 0, ts = 0;
+    for (int64_t i = 0; i < n_config; ++i) {
+        th += ch[i];
+        ts += cs[i];
+    }
+    B.nnzH = th;
+    B.nnzS = ts;
+    B.sig = sig;
+    if ((int64_t)ref[0] != th || (int64_t)ref[1] != ts) {
+        B.sig = 0;
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "count_nnz contract broken for this block: construct gives nnz_H=%lld nnz_S=%lld, "
+                 "count_nnz gives %lld %lld",
+                 (long long)th, (long long)ts, (long long)ref[0], (long long)ref[1]);
+        return fail(h, BS2E_ERR_COUNT, buf);
+    }
+    return BS2E_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+BS2E_API void bs2e_default_opts(bs2e_opts *o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->precision = BS2E_PREC_FP64;
+    o->device = 0;
+}
+
+BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
+                                 int64_t max_k, const bs2e_opts *opts, bs2e_handle **out) {
+    if (!out || !knots) return BS2E_ERR_ARG;
+    *out = nullptr;
+    if (k < 2 || k > kMaxOrder || k_GL < 1 || k_GL > kMaxGL || max_k < 0 || max_k + 1 > kMaxK1)
+        return BS2E_ERR_ARG;
+    int64_t n = n_knots - k;
+    if (n - 2 < 1 || n_knots - 2 * k + 1 < 1) return BS2E_ERR_ARG;
+    for (int64_t i = 1; i < n_knots; ++i)
+        if (!(knots[i] >= knots[i - 1])) return BS2E_ERR_ARG;
+    // every breakpoint interval must have positive length
+    for (int64_t iv = 0; iv < n_knots - 2 * k + 1; ++iv)
+        if (!(knots[k + iv] > knots[k - 1 + iv])) return BS2E_ERR_ARG;
+    bs2e_opts o;
+    bs2e_default_opts(&o);
+    if (opts) o = *opts;
+    if (o.precision != BS2E_PREC_FP64 && o.precision != BS2E_PREC_MIXED) return BS2E_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BS2E_ERR_NODEV;
+    if (o.device < 0 || o.device >= ndev) return BS2E_ERR_ARG;
+    bs2e_handle *h = new (std::nothrow) bs2e_handle();
+    if (!h) return BS2E_ERR_NOMEM;
+    h->device = (int)o.device;
+    h->precision = (int)o.precision;
+    cudaSetDevice(h->device);
+    Radial &g = h->g;
+    g.k = (int)k;
+    g.q = (int)k_GL;
+    g.K1 = (int)max_k + 1;
+    g.n_knots = (int)n_knots;
+    g.n = (int)n;
+    g.N = (int)n - 2;
+    g.n_iv = (int)(n_knots - 2 * k + 1);
+    g.W = 2 * g.k - 1;
+    g.tile = ((int64_t)g.K1 * g.W * g.W + 1) / 2 * 2;
+    h->knots.assign(knots, knots + n_knots);
+    h->glx.resize(g.q);
+    h->glw.resize(g.q);
+    gauss_legendre(g.q, h->glx.data(), h->glw.data());
+    h->rk_done.assign(g.K1, 0);
+    bs2e_status st = BS2E_OK;
+    auto bad = [&](cudaError_t e) {
+        if (e != cudaSuccess && st == BS2E_OK)
+            st = (e == cudaErrorMemoryAllocation) ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA;
+    };
+    bad(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    size_t q = g.q, kk = g.k, niv = g.n_iv, K1 = g.K1;
+    bad(dalloc(&h->d_knots, (size_t)n_knots));
+    bad(dalloc(&h->d_glx, q));
+    bad(dalloc(&h->d_glw, q));
+    bad(dalloc(&h->d_tab_r, niv * q));
+    bad(dalloc(&h->d_tab_B, niv * q * kk));
+    bad(dalloc(&h->d_tab_ri, niv * q * q));
+    bad(dalloc(&h->d_tab_Bi, niv * q * q * kk));
+    bad(dalloc(&h->d_mom, niv * K1 * 2 * kk * kk));
+    bad(dalloc(&h->d_dint, niv * K1 * kk * kk * kk * kk));
+    bad(dalloc(&h->d_tot, (size_t)2 * K1 * g.N * g.W));
+    bad(dalloc(&h->d_err, 1));
+    if (st == BS2E_OK) {
+        bad(cudaMemcpy(h->d_knots, knots, sizeof(double) * n_knots, cudaMemcpyHostToDevice));
+        bad(cudaMemcpy(h->d_glx, h->glx.data(), sizeof(double) * q, cudaMemcpyHostToDevice));
+        bad(cudaMemcpy(h->d_glw, h->glw.data(), sizeof(double) * q, cudaMemcpyHostToDevice));
+        bad(cudaMemset(h->d_err, 0, sizeof(int)));
+    }
+    if (st == BS2E_OK && (moments_smem(g) > 200 * 1024 || fill_smem(g) > 200 * 1024))
+        st = BS2E_ERR_ARG;
+    if (st != BS2E_OK) {
+        bs2e_destroy(h);
+        return st;
+    }
+    *out = h;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
+    if (!h) return BS2E_OK;
+    {
+        std::lock_guard<std::mutex> lk(h->mu);
+        cudaSetDevice(h->device);
+        if (h->stream) cudaStreamSynchronize(h->stream);
+        free_block(h->blk);
+        dfree(h->d_knots);
+        dfree(h->d_glx);
+        dfree(h->d_glw);
+        dfree(h->d_tab_r);
+        dfree(h->d_tab_B);
+        dfree(h->d_tab_ri);
+        dfree(h->d_tab_Bi);
+        dfree(h->d_mom);
+        dfree(h->d_dint);
+        dfree(h->d_tot);
+        dfree(h->d_R);
+        dfree(h->d_Rf);
+        dfree(h->d_Rexp);
+        dfree(h->d_err);
+        dfree(h->d_Hb);
+        dfree(h->d_Sb);
+        if (h->stream) cudaStreamDestroy(h->stream);
+    }
+    delete h;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_last_error(const bs2e_handle *h, char *buf, int64_t len) {
+    if (!h || !buf || len <= 0) return BS2E_ERR_ARG;
+    size_t n = std::min((size_t)len - 1, h->err.size());
+    memcpy(buf, h->err.data(), n);
+    buf[n] = 0;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_sizes(const bs2e_handle *h, int64_t *n_b, int64_t *n_iv, int64_t *nnz4,
+                                int64_t *nnz6) {
+    if (!h) return BS2E_ERR_ARG;
+    const Radial &g = h->g;
+    int64_t s4 = 0, s6 = 0;
+    for (int iv = 0; iv < g.n_iv; ++iv) {
+        int64_t c = splines_on(g, iv);
+        s4 += c * c;
+        s6 += c * c * c * c;
+    }
+    if (n_b) *n_b = g.N;
+    if (n_iv) *n_iv = g.n_iv;
+    if (nnz4) *nnz4 = s4;
+    if (nnz6) *nnz6 = s6;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_slater(bs2e_handle *h) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard G(h);
+    launch_tabulate(h);
+    launch_moments(h);
+    launch_totals(h);
+    TRY(sync_check(h, "slater"));
+    h->slater_done = true;
+    std::fill(h->rk_done.begin(), h->rk_done.end(), 0);
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_get_primitives(bs2e_handle *h, double *r_k, double *r_m_k,
+                                         int64_t *idx4, double *r_d_k, int64_t *idx6) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard G(h);
+    if (!h->slater_done) return fail(h, BS2E_ERR_STATE, "bs2e_slater has not run");
+    const Radial &g = h->g;
+    const int k = g.k, K1 = g.K1, N = g.N, k2 = k * k;
+    int64_t nnz4 = 0, nnz6 = 0;
+    bs2e_sizes(h, nullptr, nullptr, &nnz4, &nnz6);
+    std::vector<double> mom((size_t)g.n_iv * K1 * 2 * k2);
+    CU(cudaMemcpy(mom.data(), h->d_mom, mom.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    auto ivrange = [&](int a, int c, int &lo, int &hi) {  // 0-based basis -> 0-based intervals
+        lo = std::max(std::max(a, c) - k + 2, 0);
+        hi = std::min(std::min(a, c) + 1, g.n_iv - 1);
+    };
+    if (r_k || r_m_k || idx4) {
+        int64_t p = 0;
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                if (std::abs(i - j) >= k) continue;
+                int lo, hi;
+                ivrange(i, j, lo, hi);
+                for (int iv = lo; iv <= hi; ++iv, ++p) {
+                    int si = i + 1 - iv, sj = j + 1 - iv;
+                    for (int kk = 0; kk < K1; ++kk) {
+                        const double *m = mom.data() + ((size_t)iv * K1 + kk) * 2 * k2;
+                        if (r_k) r_k[p + nnz4 * kk] = m[si * k + sj];
+                        if (r_m_k) r_m_k[p + nnz4 * kk] = m[k2 + si * k + sj];
+                    }
+                    if (idx4) {
+                        idx4[3 * p] = iv + 1;
+                        idx4[3 * p + 1] = i + 1;
+                        idx4[3 * p + 2] = j + 1;
+                    }
+                }
+            }
+    }
+    if (r_d_k || idx6) {
+        std::vector<double> dint((size_t)g.n_iv * K1 * k2 * k2);
+        CU(cudaMemcpy(dint.data(), h->d_dint, dint.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        int64_t p = 0;
+        for (int jp = 0; jp < N; ++jp)
+            for (int j = std::max(0, jp - k + 1); j <= std::min(N - 1, jp + k - 1); ++j)
+                for (int ip = 0; ip < N; ++ip)
+                    for (int i = std::max(0, ip - k + 1); i <= std::min(N - 1, ip + k - 1); ++i) {
+                        int lo1, hi1, lo2, hi2;
+                        ivrange(i, ip, lo1, hi1);
+                        ivrange(j, jp, lo2, hi2);
+                        for (int iv = std::max(lo1, lo2); iv <= std::min(hi1, hi2); ++iv, ++p) {
+                            int pp = (i + 1 - iv) * k + (ip + 1 - iv);
+                            int qq = (j + 1 - iv) * k + (jp + 1 - iv);
+                            if (r_d_k)
+                                for (int kk = 0; kk < K1; ++kk)
+                                    r_d_k[p + nnz6 * kk] =
+                                        dint[(((size_t)iv * K1 + kk) * k2 + pp) * k2 + qq];
+                            if (idx6) {
+                                int64_t *e = idx6 + 5 * p;
+                                e[0] = iv + 1;
+                                e[1] = i + 1;
+                                e[2] = ip + 1;
+                                e[3] = j + 1;
+                                e[4] = jp + 1;
+                            }
+                        }
+                    }
+    }
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_rk(bs2e_handle *h, int64_t k_first, int64_t k_count) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard G(h);
+    const Radial &g = h->g;
+    if (!h->slater_done) return fail(h, BS2E_ERR_STATE, "bs2e_slater has not run");
+    if (k_first < 0 || k_count < 1 || k_first + k_count > g.K1)
+        return fail(h, BS2E_ERR_ARG, "multipole range out of bounds");
+    if (!h->d_R) CU(dalloc(&h->d_R, (size_t)g.N * g.N * g.tile));
+    launch_rk_fill(h, (int)k_first, (int)k_count);
+    TRY(sync_check(h, "rk"));
+    for (int64_t kk = k_first; kk < k_first + k_count; ++kk) h->rk_done[kk] = 1;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t *keys,
+                                       double *vals) {
+    if (!h || n < 0 || (n > 0 && (!keys || !vals))) return BS2E_ERR_ARG;
+    Guard G(h);
+    if (!h->d_R) return fail(h, BS2E_ERR_STATE, "bs2e_rk has not run");
+    if (n == 0) return BS2E_OK;
+    int64_t *dk = nullptr;
+    double *dv = nullptr;
+    CU(dalloc(&dk, (size_t)4 * n));
+    CU(dalloc(&dv, (size_t)n * h->g.K1));
+    CU(cudaMemcpyAsync(dk, keys, sizeof(int64_t) * 4 * n, cudaMemcpyHostToDevice, h->stream));
+    launch_rk_gather(h, n, dk, dv);
+    CU(cudaMemcpyAsync(vals, dv, sizeof(double) * n * h->g.K1, cudaMemcpyDeviceToHost, h->stream));
+    bs2e_status st = sync_check(h, "rk_get");
+    cudaFree(dk);
+    cudaFree(dv);
+    return st;
+}
+
+BS2E_API bs2e_status bs2e_rk_get(bs2e_handle *h, const int64_t key[4], double *vals) {
+    return bs2e_rk_get_batch(h, 1, key, vals);
+}
+
+BS2E_API bs2e_status bs2e_set_one_body(bs2e_handle *h, const double *H1p, int64_t n_l,
+                                       const double *S) {
+    if (!h || !H1p || !S || n_l < 1 || n_l > 32) return BS2E_ERR_ARG;
+    Guard G(h);
+    const Radial &g = h->g;
+    const int N = g.N, W = g.W, k = g.k;
+    std::vector<double2> Hb((size_t)n_l * N * W), Sb((size_t)N * W);
+    bool sreal = true;
+    for (int x = 0; x < N; ++x)
+        for (int d = 0; d < W; ++d) {
+            int y = x + d - (k - 1);
+            double2 sv = make_double2(0.0, 0.0);
+            if (y >= 0 && y < N) {
+                size_t o = ((size_t)y * N + x) * 2;  // column-major (x, y)
+                sv = make_double2(S[o], S[o + 1]);
+                if (S[o + 1] != 0.0) sreal = false;
+            }
+            Sb[(size_t)x * W + d] = sv;
+            for (int l = 0; l < n_l; ++l) {
+                double2 hv = make_double2(0.0, 0.0);
+                if (y >= 0 && y < N) {
+                    size_t o = (((size_t)l * N + y) * N + x) * 2;
+                    hv = make_double2(H1p[o], H1p[o + 1]);
+                }
+                Hb[((size_t)l * N + x) * W + d] = hv;
+            }
+        }
+    dfree(h->d_Hb);
+    dfree(h->d_Sb);
+    CU(dalloc(&h->d_Hb, Hb.size()));
+    CU(dalloc(&h->d_Sb, Sb.size()));
+    CU(cudaMemcpy(h->d_Hb, Hb.data(), Hb.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(h->d_Sb, Sb.data(), Sb.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    h->n_l = n_l;
+    h->s_real = sreal;
+    h->have_one_body = true;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order,
+                                   double cap_r0, double cap_eta_re, double cap_eta_im, double *H1p,
+                                   double *S) {
+    if (!h || n_l < 1 || n_l > 32 || cap_order < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    const Radial &g = h->g;
+    const int N = g.N, W = g.W, k = g.k;
+    dfree(h->d_Hb);
+    dfree(h->d_Sb);
+    CU(dalloc(&h->d_Hb, (size_t)n_l * N * W));
+    CU(dalloc(&h->d_Sb, (size_t)N * W));
+    launch_one_body(h, Z, n_l, cap_order, cap_r0, cap_eta_re, cap_eta_im);
+    TRY(sync_check(h, "one_body"));
+    h->n_l = n_l;
+    h->s_real = true;
+    h->have_one_body = true;
+    if (H1p || S) {
+        std::vector<double2> Hb((size_t)n_l * N * W), Sb((size_t)N * W);
+        CU(cudaMemcpy(Hb.data(), h->d_Hb, Hb.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+        CU(cudaMemcpy(Sb.data(), h->d_Sb, Sb.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+        if (S) memset(S, 0, sizeof(double) * 2 * (size_t)N * N);
+        if (H1p) memset(H1p, 0, sizeof(double) * 2 * (size_t)n_l * N * N);
+        for (int x = 0; x < N; ++x)
+            for (int d = 0; d < W; ++d) {
+                int y = x + d - (k - 1);
+                if (y < 0 || y >= N) continue;
+                if (S) {
+                    size_t o = ((size_t)y * N + x) * 2;
+                    S[o] = Sb[(size_t)x * W + d].x;
+                    S[o + 1] = Sb[(size_t)x * W + d].y;
+                }
+                if (H1p)
+                    for (int l = 0; l < n_l; ++l) {
+                        size_t o = (((size_t)l * N + y) * N + x) * 2;
+                        H1p[o] = Hb[((size_t)l * N + x) * W + d].x;
+                        H1p[o + 1] = Hb[((size_t)l * N + x) * W + d].y;
+                    }
+            }
+    }
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_block_count_ex(bs2e_handle *h, const bs2e_config *configs,
+                                         int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                         int64_t *nnz_H, int64_t *nnz_S) {
+    if (!h || !nnz_H || !nnz_S || n_config < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    TRY(ensure_counted(h, configs, n_config, L, spin, full));
+    *nnz_H = h->blk.nnzH;
+    *nnz_S = h->blk.nnzS;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_block_count(bs2e_handle *h, const bs2e_config *configs,
+                                      int64_t n_config, int64_t L, int64_t full, int64_t *nnz_H,
+                                      int64_t *nnz_S) {
+    return bs2e_block_count_ex(h, configs, n_config, L, 0, full, nnz_H, nnz_S);
+}
+
+BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *configs,
+                                        int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                        int64_t *H_index_ptr, int64_t *H_indices, double *H_data,
+                                        int64_t *S_index_ptr, int64_t *S_indices, double *S_data,
+                                        int64_t out_on_device) {
+    if (!h || n_config < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    for (int kk = 0; kk < h->g.K1; ++kk)
+        if (!h->rk_done[kk]) return fail(h, BS2E_ERR_STATE, "bs2e_rk has not built every multipole");
+    if (!h->have_one_body)
+        return fail(h, BS2E_ERR_STATE, "one-body matrices not set (bs2e_set_one_body / bs2e_one_body)");
+    TRY(ensure_counted(h, configs, n_config, L, spin, full));
+    for (int c = 0; c < h->plan.n_ch; ++c)
+        if (h->plan.ch_l1[c] >= h->n_l || h->plan.ch_l2[c] >= h->n_l)
+            return fail(h, BS2E_ERR_ARG, "one-body matrices do not cover every l of the block");
+    const int64_t nH = h->blk.nnzH, nS = h->blk.nnzS;
+    if (!H_index_ptr || !S_index_ptr || (nH > 0 && (!H_indices || !H_data)) ||
+        (nS > 0 && (!S_indices || !S_data)))
+        return fail(h, BS2E_ERR_ARG, "NULL output array");
+    int64_t *dHp, *dSp, *dHi, *dSi;
+    double2 *dHd, *dSd;
+    bool dev = out_on_device != 0;
+    if (dev) {
+        dHp = H_index_ptr;
+        dSp = S_index_ptr;
+        dHi = H_indices;
+        dSi = S_indices;
+        dHd = (double2 *)H_data;
+        dSd = (double2 *)S_data;
+    } else {
+        CU(dalloc(&dHp, (size_t)n_config + 1));
+        CU(dalloc(&dSp, (size_t)n_config + 1));
+        CU(dalloc(&dHi, (size_t)nH));
+        CU(dalloc(&dSi, (size_t)nS));
+        CU(dalloc(&dHd, (size_t)nH));
+        CU(dalloc(&dSd, (size_t)nS));
+    }
+    launch_block_scan(h, dHp, dSp);
+    launch_block_fill(h, dHp, dSp, dHi, dHd, dSi, dSd);
+    bs2e_status st = BS2E_OK;
+    if (!dev) {
+        cudaError_t e = cudaSuccess;
+        auto cp = [&](void *dst, const void *src, size_t bytes) {
+            if (e == cudaSuccess && bytes)
+                e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
+        };
+        cp(H_index_ptr, dHp, sizeof(int64_t) * (n_config + 1));
+        cp(S_index_ptr, dSp, sizeof(int64_t) * (n_config + 1));
+        cp(H_indices, dHi, sizeof(int64_t) * nH);
+        cp(H_data, dHd, sizeof(double2) * nH);
+        cp(S_indices, dSi, sizeof(int64_t) * nS);
+        cp(S_data, dSd, sizeof(double2) * nS);
+        if (e != cudaSuccess) st = fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+    }
+    bs2e_status st2 = sync_check(h, "block fill");
+    if (!dev) {
+        cudaFree(dHp);
+        cudaFree(dSp);
+        cudaFree(dHi);
+        cudaFree(dSi);
+        cudaFree(dHd);
+        cudaFree(dSd);
+    }
+    return st != BS2E_OK ? st : st2;
+}
+
+BS2E_API bs2e_status bs2e_block_fill(bs2e_handle *h, const bs2e_config *configs,
+                                     int64_t n_config, int64_t L, int64_t full, const double *H1p,
+                                     int64_t n_l, const double *S, int64_t *H_index_ptr,
+                                     int64_t *H_indices, double *H_data, int64_t *S_index_ptr,
+                                     int64_t *S_indices, double *S_data) {
+    if (!h) return BS2E_ERR_ARG;
+    if (H1p || S) {
+        if (!H1p || !S) return BS2E_ERR_ARG;
+        bs2e_status st = bs2e_set_one_body(h, H1p, n_l, S);
+        if (st != BS2E_OK) return st;
+    }
+    return bs2e_block_fill_ex(h, configs, n_config, L, 0, full, H_index_ptr, H_indices, H_data,
+                              S_index_ptr, S_indices, S_data, 0);
+}
+
+BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream) {
+    if (!h || !stream) return BS2E_ERR_ARG;
+    *stream = (void *)h->stream;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_launch_count(const bs2e_handle *h, int64_t *count) {
+    if (!h || !count) return BS2E_ERR_ARG;
+    *count = h->launches;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_synchronize(bs2e_handle *h) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard G(h);
+    return sync_check(h, "synchronize");
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// bs2e_internal.h -- shared declarations of the GB300 two-electron library.
+//
+// Data layout in HBM (0-based indices; N = n_b basis splines, W = 2k-1,
+// K1 = max_k+1, q = k_GL points per interval, n_iv breakpoint intervals):
+//   tab_r   [n_iv][q]           outer quadrature radii of each interval
+//   tab_B   [n_iv][q][k]        values of the k splines non-zero on the interval
+//   tab_ri  [n_iv][q][q]        inner radii on [t_iv, r_P] for every outer point P
+//   tab_Bi  [n_iv][q][q][k]     spline values at the inner radii
+//   mom     [n_iv][K1][2][k][k] per-interval moments (0: int B B r^k, 1: int B B r^-(k+1))
+//   dint    [n_iv][K1][k*k][k*k] same-interval 2-D integrals D(p=(i,i'), q=(j,j'))
+//   tot     [2][K1][N][W]       moments summed over all shared intervals of a pair
+//   R       [N][N][tile]        R^k store, tile = [K1][W][W] padded to 16 bytes:
+//                               R^k[a,b,c,d] at tile(a,b)[k][c-a+k-1][d-b+k-1]
+// Band pairs (a,c) with |a-c|<k share the intervals [max(a,c)-k+2, min(a,c)+1]
+// (clipped to [0,n_iv)); spline b0 is local index s = b0+1-iv on interval iv.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bs2e.h"
+
+namespace bs2e {
+
+constexpr int kMaxOrder = 16;  // B-spline order limit (the reference allows 20 in BVALUE_D)
+constexpr int kMaxGL = 32;     // Gauss-Legendre points per interval
+constexpr int kMaxK1 = 32;     // multipoles 0..31
+
+// Per (row channel, column channel) coupling of one symmetry block.
+struct PairInfo {
+    int32_t flags;   // bit0 dir_ok, bit1 ex_ok, bit2 l_eq, bit3 l_eq_ex
+    int32_t nd, nx;  // lengths of the direct / exchange multipole lists
+    int32_t pad;
+    double sgn;      // exchange sign (-1)^(l_c+l_d+L) (times -1 for the triplet)
+};
+
+// Host-side plan of one symmetry block (built from the configuration list).
+struct BlockPlan {
+    int64_t n_config = 0, L = 0, spin = 0, full = 1;
+    int n_ch = 0;
+    std::vector<int> ch_l1, ch_l2;          // channel angular momenta
+    std::vector<int> row_n1, row_n2, row_ch;  // per row
+    // per channel c and n1 in [0, N+1]: first config row, n2 range (hi < lo = empty)
+    std::vector<int> seg_base, seg_lo, seg_hi;  // [n_ch][N+2]
+    std::vector<PairInfo> pairs;                // [n_ch][n_ch]
+    std::vector<int8_t> pair_k;                 // [n_ch][n_ch][2][K1]
+    std::vector<double> pair_a;                 // [n_ch][n_ch][2][K1]
+    std::vector<float> pair_af;                 // [n_ch][n_ch][2][K1][2] (hi, lo) for the mixed path
+    // tiles: distinct (n_a, n_b) with their rows
+    std::vector<int> tile_a, tile_b, tile_ptr, tile_rows;
+    bool count_mismatch = false;  // a channel pair where count_nnz and construct differ
+};
+
+// Device copy of a block plan.
+struct DevBlock {
+    int4 *rows = nullptr;  // (n1, n2, ch, 0) per row, 1-based n
+    int *seg = nullptr;    // base | lo | hi, each [n_ch][N+2]
+    PairInfo *pairs = nullptr;
+    int8_t *pair_k = nullptr;
+    double *pair_a = nullptr;
+    float *pair_af = nullptr;
+    int *tile_ab = nullptr;  // [n_tiles][2]
+    int *tile_ptr = nullptr;
+    int *tile_rows = nullptr;
+    int64_t *cntH = nullptr, *cntS = nullptr;  // per-row counts, then exclusive offsets
+    int64_t *scan_tmp = nullptr;
+    int64_t n_tiles = 0;
+    int64_t nnzH = -1, nnzS = -1;
+    // identity of the counted block
+    uint64_t sig = 0;
+    std::vector<char> bytes;  // owning allocation bookkeeping
+};
+
+struct Radial {
+    int k = 0, q = 0, K1 = 0, N = 0, n_iv = 0, W = 0, n = 0, n_knots = 0;
+    int64_t tile = 0;  // padded doubles per R tile
+};
+
+}  // namespace bs2e
+
+struct bs2e_handle {
+    std::mutex mu;
+    std::string err;
+    int device = 0;
+    int precision = 0;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+    bs2e::Radial g;
+    std::vector<double> knots, glx, glw;
+    // device radial data
+    double *d_knots = nullptr, *d_glx = nullptr, *d_glw = nullptr;
+    double *d_tab_r = nullptr, *d_tab_B = nullptr, *d_tab_ri = nullptr, *d_tab_Bi = nullptr;
+    double *d_mom = nullptr, *d_dint = nullptr, *d_tot = nullptr;
+    double *d_R = nullptr;      // FP64 store
+    float2 *d_Rf = nullptr;     // mixed store: scaled (hi, lo) pairs, same tile layout
+    int32_t *d_Rexp = nullptr;  // mixed store: power-of-two scale per (tile, k)
+    int *d_err = nullptr;       // device error word (bounded waits)
+    bool slater_done = false;
+    std::vector<char> rk_done;  // per k
+    // one-body, banded complex: Hb[l][x][W], Sb[x][W]
+    double2 *d_Hb = nullptr, *d_Sb = nullptr;
+    int64_t n_l = 0;
+    bool have_one_body = false;
+    bool s_real = true;
+    // block cache
+    bs2e::BlockPlan plan;
+    bs2e::DevBlock blk;
+};
+
+namespace bs2e {
+
+// Host helpers (bs2e_angular.cpp, bs2e_basis.cpp)
+double ang_k_LS(int k, int la, int lb, int lc, int ld, int L);
+double three_j(int ja, int jb, int jc, int ma, int mb, int mc);
+double six_j(int ja, int jb, int jc, int jd, int je, int jf);
+void gauss_legendre(int q, double *x, double *w);
+// Builds the block plan; returns BS2E_OK or an error code with message.
+bs2e_status build_plan(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
+                       int64_t full, const Radial &g, BlockPlan &plan, std::string &err);
+
+// Kernel launchers (bs2e_radial.cu)
+void launch_tabulate(bs2e_handle *h);
+void launch_moments(bs2e_handle *h);
+void launch_totals(bs2e_handle *h);
+void launch_rk_fill(bs2e_handle *h, int k_first, int k_count);
+void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *d_vals);
+void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, double cap_r0,
+                     double eta_re, double eta_im);
+// Kernel launchers (bs2e_assembly.cu)
+void launch_block_count(bs2e_handle *h);
+void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr);
+void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_Sptr,
+                       int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx, double2 *d_Sdat);
+
+}  // namespace bs2e

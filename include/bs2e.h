@@ -1,0 +1,196 @@
+/*
+ * bs2e.h -- C ABI of the GB300 two-electron matrix-element library.
+ *
+ * Drop-in for the two-electron path that basis_setup runs in
+ * edvinolo/b-spline-two-e (src/apps/main_basis_setup.f90:77-85 and :105-116):
+ * radial Slater-integral primitives, the R^k[a,b,c,d] store, the 3j/6j
+ * angular weights and the sparse CSR assembly of every symmetry block of the
+ * two-electron Hamiltonian H and overlap S.  The Fortran host binds these
+ * entry points through ISO_C_BINDING; nothing here uses C++ or torch types.
+ *
+ * Conventions (all follow the reference, which is built with
+ * -fdefault-integer-8):
+ *   - every integer is int64_t; basis, interval and configuration indices are
+ *     1-based (Fortran numbering) wherever they cross this boundary;
+ *   - 2-D arrays are column-major;
+ *   - "complex" arrays are complex128 stored as interleaved (re, im) doubles,
+ *     i.e. Fortran complex(c_double_complex);
+ *   - CSR output is the reference's CSR_matrix layout
+ *     (src/tools/sparse_array_tools.f90:63-135): index_ptr(rows+1) and
+ *     indices(nnz) 1-based, columns ascending within a row, data complex128.
+ *
+ * Every call returns a bs2e_status; BS2E_OK is 0.  On error the handle keeps
+ * a message readable with bs2e_last_error().  Calls on one handle are
+ * serialised by an internal mutex, so a Fortran OpenMP loop may call the
+ * block entry points concurrently (as main_basis_setup.f90:105 does).
+ */
+#ifndef BS2E_H
+#define BS2E_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define BS2E_API __attribute__((visibility("default")))
+#else
+#define BS2E_API
+#endif
+
+typedef int32_t bs2e_status;
+
+enum {
+    BS2E_OK = 0,
+    BS2E_ERR_ARG = 1,     /* invalid argument (sizes, knots, ranges) */
+    BS2E_ERR_NOMEM = 2,   /* device or host allocation failed */
+    BS2E_ERR_CUDA = 3,    /* CUDA runtime error */
+    BS2E_ERR_COUNT = 4,   /* count/fill disagreement (reference count_nnz contract broken) */
+    BS2E_ERR_TIMEOUT = 5, /* a bounded device wait gave up */
+    BS2E_ERR_STATE = 6,   /* call made out of order (e.g. fill before bs2e_rk) */
+    BS2E_ERR_NODEV = 7,   /* no CUDA device available */
+    BS2E_ERR_ORDER = 8    /* configuration list is not in basis order */
+};
+
+/* Arithmetic used for the R^k store and the sum over multipoles. */
+enum {
+    BS2E_PREC_FP64 = 0,  /* plain path: every operation in FP64 */
+    BS2E_PREC_MIXED = 1  /* R^k stored as scaled FP32 pairs, k-sum in FP32-pair arithmetic */
+};
+
+typedef struct bs2e_handle bs2e_handle;
+
+typedef struct {
+    int64_t precision; /* BS2E_PREC_FP64 (default) or BS2E_PREC_MIXED */
+    int64_t device;    /* CUDA device ordinal (default 0) */
+    int64_t reserved[6];
+} bs2e_opts;
+
+/* One two-electron configuration: type(config) of src/tools/orbital_tools.f90:15-19
+ * as a bind(C) record (n(2), l(2), eqv as int64). */
+typedef struct {
+    int64_t n1, n2;
+    int64_t l1, l2;
+    int64_t eqv;
+} bs2e_config;
+
+/* Fills *opts with defaults (FP64, device 0). */
+BS2E_API void bs2e_default_opts(bs2e_opts *opts);
+
+/* Creates a handle for one B-spline basis.  Replaces splines%init(k,grid)
+ * (src/tools/bspline_tools.f90:27-40) together with the r_k/r_m_k/r_d_k%init
+ * calls of main_basis_setup.f90:77-79: knots is the full knot vector t(1:n+k),
+ * n_b = n-2 splines are kept (first and last dropped), k_GL Gauss-Legendre
+ * points per breakpoint interval, multipoles k = 0..max_k. */
+BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
+                                 int64_t max_k, const bs2e_opts *opts, bs2e_handle **out);
+
+BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h);
+
+/* Copies the last error message (NUL-terminated, truncated to len). */
+BS2E_API bs2e_status bs2e_last_error(const bs2e_handle *h, char *buf, int64_t len);
+
+/* Basis size n_b, interval count and the COO sizes nnz4/nnz6 of the
+ * reference's sparse_4d / sparse_6d primitives (sparse_array_tools.f90:276-324). */
+BS2E_API bs2e_status bs2e_sizes(const bs2e_handle *h, int64_t *n_b, int64_t *n_iv, int64_t *nnz4,
+                                int64_t *nnz6);
+
+/* Slater primitives on the device.  Replaces setup_Slater_integrals
+ * (src/mat_els/mat_els.f90:172-292): per-interval moments r_k, r_m_k and the
+ * same-interval kink-split 2-D integrals r_d_k for k = 0..max_k. */
+BS2E_API bs2e_status bs2e_slater(bs2e_handle *h);
+
+/* Copies the primitives out in the reference's COO order (for parity checks):
+ * r_k, r_m_k: nnz4 x (max_k+1); idx4: 3 x nnz4 = (iv, i, j);
+ * r_d_k: nnz6 x (max_k+1); idx6: 5 x nnz6 = (iv, i, i_p, j, j_p).
+ * Any pointer may be NULL to skip that array. */
+BS2E_API bs2e_status bs2e_get_primitives(bs2e_handle *h, double *r_k, double *r_m_k,
+                                         int64_t *idx4, double *r_d_k, int64_t *idx6);
+
+/* Builds the R^k store for multipoles k_first .. k_first+k_count-1 (pass 0 and
+ * max_k+1 for all).  Replaces compute_R_k_map (src/tools/sparse_array_tools.f90:452-493). */
+BS2E_API bs2e_status bs2e_rk(bs2e_handle *h, int64_t k_first, int64_t k_count);
+
+/* R^k values of one key [a,b,c,d] (1-based, |a-c|<k, |b-d|<k) for k = 0..max_k,
+ * as Nd_DOK%get_val (src/tools/sparse_array_tools.f90:536-555). */
+BS2E_API bs2e_status bs2e_rk_get(bs2e_handle *h, const int64_t key[4], double *vals);
+
+/* Batched bs2e_rk_get: keys is 4 x n column-major, vals is (max_k+1) x n. */
+BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t *keys,
+                                       double *vals);
+
+/* Uploads the one-body matrices used by every block: H1p is n_b x n_b x n_l
+ * complex (H_vec(l)%data for l = 0..n_l-1, main_basis_setup.f90:95-99), S is
+ * n_b x n_b complex (main_basis_setup.f90:91-93). */
+BS2E_API bs2e_status bs2e_set_one_body(bs2e_handle *h, const double *H1p, int64_t n_l,
+                                       const double *S);
+
+/* Computes the one-body matrices on the device instead (setup_S and
+ * setup_H_one_particle, src/mat_els/mat_els.f90:47-118, hydrogenic potential
+ * potentials.f90:35-43 and the CAP of CAP_tools.f90:23-33), keeps them for the
+ * blocks and optionally copies them out (H1p / S may be NULL). */
+BS2E_API bs2e_status bs2e_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order,
+                                   double cap_r0, double cap_eta_re, double cap_eta_im,
+                                   double *H1p, double *S);
+
+/* Number of non-zeros of the H and S blocks of one symmetry (L, singlet).
+ * Same contract as count_nnz (src/mat_els/hamiltonian.f90:348-416): the counts
+ * size the CSR arrays that bs2e_block_fill writes.  full = 1 gives the whole
+ * block, full = 0 the upper triangle (hamiltonian.f90:131-135). */
+BS2E_API bs2e_status bs2e_block_count(bs2e_handle *h, const bs2e_config *configs,
+                                      int64_t n_config, int64_t L, int64_t full, int64_t *nnz_H,
+                                      int64_t *nnz_S);
+
+/* Fills one symmetry block into caller-allocated host arrays sized by
+ * bs2e_block_count.  Replaces construct_block_tensor
+ * (src/mat_els/hamiltonian.f90:106-283).  H1p / S may be NULL to use the
+ * matrices set by bs2e_set_one_body / bs2e_one_body. */
+BS2E_API bs2e_status bs2e_block_fill(bs2e_handle *h, const bs2e_config *configs,
+                                     int64_t n_config, int64_t L, int64_t full, const double *H1p,
+                                     int64_t n_l, const double *S, int64_t *H_index_ptr,
+                                     int64_t *H_indices, double *H_data, int64_t *S_index_ptr,
+                                     int64_t *S_indices, double *S_data);
+
+/* Extended forms.  spin = 0 is the reference's singlet coupling; spin = 1
+ * builds the triplet block (exchange terms change sign; equivalent
+ * configurations belong to odd L), which the reference does not have.
+ * out_on_device = 1 means the six output pointers are CUDA device pointers
+ * (inputs already resident in HBM); 0 means host memory. */
+BS2E_API bs2e_status bs2e_block_count_ex(bs2e_handle *h, const bs2e_config *configs,
+                                         int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                         int64_t *nnz_H, int64_t *nnz_S);
+BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *configs,
+                                        int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                        int64_t *H_index_ptr, int64_t *H_indices, double *H_data,
+                                        int64_t *S_index_ptr, int64_t *S_indices, double *S_data,
+                                        int64_t out_on_device);
+
+/* Configuration list of one symmetry block, as count_configs
+ * (src/tools/orbital_tools.f90:119-216) with consistent() (:46-72); spin as
+ * above.  Returns the count in *n_config and writes the list when out != NULL. */
+BS2E_API bs2e_status bs2e_configs(int64_t L, int64_t parity_odd, int64_t max_l_1p, int64_t n_b,
+                                  int64_t k, int64_t max_n_b, int64_t n_all_l, int64_t l2_max,
+                                  int64_t spin, bs2e_config *out, int64_t *n_config);
+
+/* ang_k_LS (src/tools/wigner_tools.f90:126-138) computed from exact rational
+ * 3j/6j sums: confs(1) = (la, lb), confs(2) = (lc, ld). */
+BS2E_API double bs2e_ang_k_LS(int64_t k, int64_t la, int64_t lb, int64_t lc, int64_t ld,
+                              int64_t L);
+/* Wigner 3j and 6j symbols of integer arguments (GSL's coupling functions as
+ * used by wigner_tools.f90:30-60). */
+BS2E_API double bs2e_three_j(int64_t ja, int64_t jb, int64_t jc, int64_t ma, int64_t mb,
+                             int64_t mc);
+BS2E_API double bs2e_six_j(int64_t ja, int64_t jb, int64_t jc, int64_t jd, int64_t je,
+                           int64_t jf);
+
+/* The CUDA stream all work of the handle runs on (cudaStream_t as void*), the
+ * number of kernels the handle has launched so far, and a full synchronize. */
+BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream);
+BS2E_API bs2e_status bs2e_launch_count(const bs2e_handle *h, int64_t *count);
+BS2E_API bs2e_status bs2e_synchronize(bs2e_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BS2E_H */
