@@ -57,26 +57,6 @@ static bool consistent(int64_t l1, int64_t l2, int64_t L, int64_t parity_odd, bo
     return par == (parity_odd != 0);
 }
 
-static uint64_t fnv(const void *p, size_t n, uint64_t h) {
-    const unsigned char *c = (const unsigned char *)p;
-    for (size_t i = 0; i < n; ++i) {
-        h ^= c[i];
-        h *= 1099511628211ull;
-    }
-    return h;
-}
-
-uint64_t plan_signature(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
-                        int64_t full) {
-    uint64_t h = 1469598103934665603ull;
-    h = fnv(&n_config, 8, h);
-    h = fnv(&L, 8, h);
-    h = fnv(&spin, 8, h);
-    h = fnv(&full, 8, h);
-    h = fnv(cf, sizeof(bs2e_config) * (size_t)n_config, h);
-    return h;
-}
-
 bs2e_status build_plan(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
                        int64_t full, const Radial &g, BlockPlan &P, std::string &err) {
     P = BlockPlan();

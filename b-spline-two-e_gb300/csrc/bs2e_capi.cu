@@ -17,8 +17,6 @@
 namespace bs2e {
 size_t moments_smem(const Radial &g);
 size_t fill_smem(const Radial &g);
-uint64_t plan_signature(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
-                        int64_t full);
 }  // namespace bs2e
 
 using namespace bs2e;
@@ -91,7 +89,7 @@ void free_block(DevBlock &b) {
     dfree(b.scan_tmp);
     b.n_tiles = 0;
     b.nnzH = b.nnzS = -1;
-    b.sig = 0;
+    b.valid = false;
 }
 
 template <class T>
@@ -115,8 +113,13 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
     if (!cf && n_config > 0) return fail(h, BS2E_ERR_ARG, "configs is NULL");
     if (L < 0 || (spin != 0 && spin != 1) || (full != 0 && full != 1))
         return fail(h, BS2E_ERR_ARG, "L, spin or full out of range");
-    uint64_t sig = plan_signature(cf, n_config, L, spin, full);
-    if (h->blk.sig == sig && h->blk.nnzH >= 0 && h->plan.n_config == n_config) return BS2E_OK;
+    {
+        const DevBlock &b = h->blk;
+        if (b.valid && b.L == L && b.spin == spin && b.full == full &&
+            (int64_t)b.cfg.size() == n_config &&
+            (n_config == 0 || memcmp(b.cfg.data(), cf, sizeof(bs2e_config) * n_config) == 0))
+            return BS2E_OK;
+    }
     free_block(h->blk);
     std::string err;
     bs2e_status st = build_plan(cf, n_config, L, spin, full, h->g, h->plan, err);
@@ -173,9 +176,7 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
     }
     B.nnzH = th;
     B.nnzS = ts;
-    B.sig = sig;
     if ((int64_t)ref[0] != th || (int64_t)ref[1] != ts) {
-        B.sig = 0;
         char buf[256];
         snprintf(buf, sizeof buf,
                  "count_nnz contract broken for this block: construct gives nnz_H=%lld nnz_S=%lld, "
@@ -183,6 +184,11 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
                  (long long)th, (long long)ts, (long long)ref[0], (long long)ref[1]);
         return fail(h, BS2E_ERR_COUNT, buf);
     }
+    B.cfg.assign(cf, cf + n_config);
+    B.L = L;
+    B.spin = spin;
+    B.full = full;
+    B.valid = true;
     return BS2E_OK;
 }
 

@@ -69,9 +69,10 @@ struct DevBlock {
     int64_t *scan_tmp = nullptr;
     int64_t n_tiles = 0;
     int64_t nnzH = -1, nnzS = -1;
-    // identity of the counted block
-    uint64_t sig = 0;
-    std::vector<char> bytes;  // owning allocation bookkeeping
+    // identity of the counted block: its parameters and a copy of its configurations
+    bool valid = false;
+    int64_t L = -1, spin = -1, full = -1;
+    std::vector<bs2e_config> cfg;
 };
 
 struct Radial {

@@ -1,0 +1,398 @@
+"""Benchmark of the two-electron matrix-element path (R^k + 2e-H assembly).
+
+Workload (the "plain FP64 GPU drop-in at medium size" configuration): helium-like
+Z=2, B-spline order 7, N=200 on the exp-linear knot grid to r_max=200 a.u.,
+10 Gauss-Legendre points per interval, multipoles k=0..10, l_max=5, total
+L=0..3 (natural parity), singlet and triplet, full blocks.  One step is the
+whole path on the GPU: Slater primitives, the R^k store, the one-body matrices
+and count + fill of all 8 symmetry blocks.
+
+value : R^k elements/s = P^2 (max_k+1) / step time, outputs written into
+        device buffers (inputs resident).  P = ordered band pairs = 2,558.
+e2e   : same metric through the C ABI with host output buffers (pinned): the
+        configuration lists go host->device and every CSR block device->host.
+roofline: the CSR fill kernel (k_fill), timed with CUDA events on the
+        library's stream; algorithmic bytes = 24 B per stored H/S entry
+        (int64 index + complex128 value) + the R^k tiles it stages.
+cpu_baseline: the CPU oracle (C restatement of the reference, OpenMP) on a
+        bounded sample: full Slater primitives + R^k map, and a row sample of
+        every block extrapolated to the full block (one thread per block, the
+        reference's OpenMP-over-symmetries decomposition).
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--precision fp64|mixed]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "R^k elements/s + 2e-H assembly s, mixed vs FP64 on GB300 at ≤1e-9 rel err"
+WORKLOAD = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5, max_L=3, Z=2, spins=(0, 1),
+                full=True, cap_order=2, cap_r0=10.0, cap_eta=1e-3)
+
+
+def _pkg():
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as ge
+    pkg = ge._package()
+    if not os.path.exists(pkg.LIB_PATH):
+        sys.path.insert(0, ge.PKG_DIR)
+        import build as b
+        b.build()
+    return pkg
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def band_pairs(k, n_b):
+    return n_b * (2 * k - 1) - k * (k - 1)
+
+
+def workload_blocks(pkg, w):
+    out = []
+    for spin in w["spins"]:
+        for (L, M, par) in pkg.basis.symmetries(w["max_L"], True):
+            cf = pkg.configs(L, par, w["l_max"], w["n_b"], w["k"], spin=spin)
+            out.append((L, par, spin, cf))
+    return out
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (oracle) on a bounded sample
+# --------------------------------------------------------------------------
+def cpu_baseline(pkg, w, rows_per_block=96, threads=None):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from concurrent.futures import ThreadPoolExecutor
+    threads = threads or os.cpu_count()
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    t0 = time.perf_counter()
+    prim = O.slater(t, w["k"], w["q"], w["max_k"], nthreads=threads)
+    t1 = time.perf_counter()
+    R = O.rk_map(w["n_b"], w["k"], w["max_k"], prim)
+    t2 = time.perf_counter()
+    H1p = O.setup_H1p(t, w["k"], w["q"], w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"],
+                      w["cap_eta"])
+    S = O.setup_S(t, w["k"], w["q"])
+    blocks = [(L, par, spin, O.count_configs(L, par, w["l_max"], w["n_b"], w["k"], spin=spin))
+              for spin in w["spins"] for (L, M, par) in pkg.basis.symmetries(w["max_L"], True)]
+
+    def run(b):
+        L, par, spin, cf = b
+        n = cf.size
+        starts = np.linspace(0, n - 1, rows_per_block).astype(np.int64)
+        ts = time.perf_counter()
+        for r in starts:
+            O.construct_block(cf, L, w["k"], w["n_b"], w["max_k"], R, H1p, S, w["full"], spin,
+                              rows=(int(r), int(r) + 1))
+        return (time.perf_counter() - ts) * n / rows_per_block
+
+    t3 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=min(threads, len(blocks))) as ex:
+        est = list(ex.map(run, blocks))
+    t4 = time.perf_counter()
+    t_full = (t1 - t0) + (t2 - t1) + max(est)
+    P = band_pairs(w["k"], w["n_b"])
+    elems = P * P * (w["max_k"] + 1)
+    return dict(value=elems / t_full, unit="R^k elements/s", cores=threads, kind="port",
+                sample=("full Slater primitives (%.1f s, OpenMP over k) + full R^k map (%.1f s, "
+                        "serial) measured; assembly extrapolated from %d evenly spaced rows of each "
+                        "of the %d blocks (%.1f s of sampling, one thread per block): full path "
+                        "%.0f s" % (t1 - t0, t2 - t1, rows_per_block, len(blocks), t4 - t3, t_full)),
+                t_full_s=t_full, t_slater_s=t1 - t0, t_rk_s=t2 - t1, t_assembly_s=max(est))
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    import torch
+    pkg = _pkg()
+    w = WORKLOAD
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    blocks = workload_blocks(pkg, w)
+    h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec, device=dev.index)
+    stream = torch.cuda.ExternalStream(h.stream, device=dev)
+
+    def radial():
+        h.slater()
+        h.rk()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+
+    radial()
+    counts = [h.block_count(cf, L, w["full"], spin) for (L, par, spin, cf) in blocks]
+    nH = sum(c[0] for c in counts)
+    nS = sum(c[1] for c in counts)
+    # device-resident outputs for every block
+    out_dev = []
+    for (L, par, spin, cf), (ch, cs) in zip(blocks, counts):
+        n = cf.size
+        Hd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
+                  indices=torch.empty(ch, dtype=torch.int64, device=dev),
+                  data=torch.empty(ch, dtype=torch.complex128, device=dev))
+        Sd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
+                  indices=torch.empty(cs, dtype=torch.int64, device=dev),
+                  data=torch.empty(cs, dtype=torch.complex128, device=dev))
+        out_dev.append((Hd, Sd))
+    ptrs = [({x: v.data_ptr() for x, v in Hd.items()}, {x: v.data_ptr() for x, v in Sd.items()})
+            for (Hd, Sd) in out_dev]
+    tile_bytes = 8 * ((w["max_k"] + 1) * (2 * w["k"] - 1) ** 2 + 1) // 2 * 2
+    n_tiles = sum(np.unique(cf["n1"] * 100000 + cf["n2"]).size for (_, _, _, cf) in blocks)
+    fill_bytes = 24 * (nH + nS) + n_tiles * tile_bytes
+
+    fill_ms = []
+
+    def step_device(record):
+        radial()
+        for b, ((L, par, spin, cf), (Hp, Sp)) in enumerate(zip(blocks, ptrs)):
+            h.block_count(cf, L, w["full"], spin)
+            if record:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            h.block_fill_into(cf, L, w["full"], spin, Hp, Sp, on_device=True)
+            if record:
+                e1.record(stream)
+                fill_ms.append((e0, e1))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step_device(False)
+    barrier()
+    launches0 = h.launch_count
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(dev.index) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step_device(True)
+        ev1.record(stream)
+        barrier()
+    launches = h.launch_count - launches0
+    t_dev = ev0.elapsed_time(ev1) / 1e3
+    fill_s = sum(a.elapsed_time(b) for a, b in fill_ms) / 1e3
+    t_dev = _max_over_ranks(t_dev, world)
+    P = band_pairs(w["k"], w["n_b"])
+    elems = P * P * (w["max_k"] + 1)
+    value = world * elems * args.steps / t_dev
+    # radial stage alone (slater + R^k + one-body), for the "+ 2e-H assembly s" split
+    barrier()
+    r0 = torch.cuda.Event(enable_timing=True)
+    r1 = torch.cuda.Event(enable_timing=True)
+    r0.record(stream)
+    for _ in range(args.steps):
+        radial()
+    r1.record(stream)
+    barrier()
+    t_radial = r0.elapsed_time(r1) / 1e3 / args.steps
+
+    # e2e through the C ABI with pinned host buffers
+    del out_dev
+    torch.cuda.empty_cache()
+    host = []
+    for (L, par, spin, cf), (ch, cs) in zip(blocks, counts):
+        n = cf.size
+        mk = lambda m, dt: torch.empty(m, dtype=dt, pin_memory=True).numpy()
+        H = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(ch, torch.int64),
+                 data=mk(ch, torch.complex128))
+        S = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(cs, torch.int64),
+                 data=mk(cs, torch.complex128))
+        host.append((H, S))
+    pinned_cfg = [torch.from_numpy(cf.view(np.int64).copy()).pin_memory().numpy().view(
+        pkg.CONFIG_DTYPE) for (_, _, _, cf) in blocks]
+    h2d = t.nbytes + sum(c.nbytes for c in pinned_cfg)
+    d2h = sum(H["index_ptr"].nbytes + H["indices"].nbytes + H["data"].nbytes +
+              S["index_ptr"].nbytes + S["indices"].nbytes + S["data"].nbytes for H, S in host)
+
+    def step_e2e():
+        radial()
+        for (L, par, spin, _), cf, (H, S) in zip(blocks, pinned_cfg, host):
+            h.block_count(cf, L, w["full"], spin)
+            h.block_fill_into(cf, L, w["full"], spin, H, S, on_device=False)
+
+    e2e_steps = max(1, min(args.steps, 3))
+    step_e2e()
+    barrier()
+    te0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step_e2e()
+    barrier()
+    t_e2e = _max_over_ranks((time.perf_counter() - te0) / e2e_steps, world)
+    e2e_value = world * elems / t_e2e
+
+    peak, peak_src = _peaks()
+    achieved = fill_bytes * args.steps / fill_s / 1e9 if fill_s > 0 else None
+    res = {
+        "metric": METRIC, "value": value, "unit": "R^k elements/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == pkg.PREC_FP64 else "f64 out, f32-pair k-sum",
+        "data": "synthetic (deterministic knot grid, no dataset)",
+        "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 "
+                               "singlet+triplet full blocks (8 blocks, %d rows)" %
+                               sum(cf.size for (_, _, _, cf) in blocks),
+                   "precision": args.precision, "nnz_H": nH, "nnz_S": nS,
+                   "rk_elements_per_step": elems,
+                   "l2": "every step writes %.1f GB of CSR (> L2)" % (24 * (nH + nS) / 1e9)},
+        "assembly_s": (t_dev / args.steps) - t_radial,
+        "radial_s": t_radial,
+        "rk_stage_elements_per_s": elems / t_radial,
+        "e2e": {"value": e2e_value, "unit": "R^k elements/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "s_per_step": t_e2e},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_fill", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_step": int(fill_bytes),
+                     "fill_s_per_step": fill_s / args.steps},
+        "clocks": clk.summary(),
+    }
+    h.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        res["cpu_baseline"] = {k: v for k, v in cpu_baseline(pkg, w).items()
+                               if k in ("value", "unit", "cores", "kind", "sample")}
+    return res
+
+
+def _max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args):
+    """The reference's algorithm on the host cores (the oracle port), same metric."""
+    pkg = _pkg()
+    w = WORKLOAD
+    for _ in range(args.warmup):
+        cpu_baseline(pkg, w, rows_per_block=8)
+    vals = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_baseline(pkg, w)
+        vals.append(last["value"])
+    v = statistics.median(vals)
+    return {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "R^k elements/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * last["t_full_s"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (deterministic knot grid, no dataset)",
+        "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 "
+                               "singlet+triplet full blocks (8 blocks)"},
+        "cpu_baseline": {"value": v, "unit": "R^k elements/s", "cores": last["cores"],
+                         "kind": "port", "sample": last["sample"]},
+        "e2e": {"value": v, "unit": "R^k elements/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    res = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
