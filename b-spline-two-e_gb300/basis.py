@@ -35,3 +35,26 @@ def symmetries(max_L, z_pol=True, two_el=True):
                     out.append((L, M, L % 2))
     assert len(out) == count_terms(max_L, z_pol, two_el)
     return out
+
+
+def block_work(n_config, n_channels):
+    """Relative assembly work of a block: rows times column channels."""
+    return int(n_config) * max(int(n_channels), 1)
+
+
+def shard_blocks(work, world_size, rank):
+    """Indices of the symmetry blocks rank `rank` assembles.
+
+    Blocks are independent (no data exchange between them), so a multi-GPU
+    basis setup hands each rank whole blocks: greedy longest-first assignment
+    to the least loaded rank, ties broken by block index so every rank
+    computes the same partition without communicating.
+    """
+    order = sorted(range(len(work)), key=lambda i: (-work[i], i))
+    load = [0] * world_size
+    owner = [0] * len(work)
+    for i in order:
+        r = min(range(world_size), key=lambda q: (load[q], q))
+        owner[i] = r
+        load[r] += work[i]
+    return [i for i in range(len(work)) if owner[i] == rank]

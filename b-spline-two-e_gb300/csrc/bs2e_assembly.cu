@@ -65,11 +65,14 @@ __device__ __forceinline__ Iv2 make_union(int a0, int a1, bool ina, int b0, int 
 }
 
 struct BlockArgs {
-    const int4 *rows;
+    const bs2e_config *cfg;                 // the configuration list (row table)
+    const int *lmap;                        // [kMaxL][kMaxL] channel of (l1, l2)
+    const int *chl;                         // [n_ch] l1 << 8 | l2
     const int *seg_base, *seg_lo, *seg_hi;  // [n_ch][N+2]
     const PairInfo *pairs;
     const int8_t *pair_k;
     const double *pair_a;
+    const float *pair_af;  // (hi, lo) FP32 pairs of pair_a
     int n_ch, N, k, K1, full, segS;
     int64_t n_rows;
 };
@@ -121,13 +124,14 @@ __device__ __forceinline__ int ovl(int a0, int a1, int b0, int b1) {
 // totals of the count_nnz predicate (hamiltonian.f90:386-413) are accumulated
 // in ref[0..1] so the host can detect a block where the two disagree.
 // ---------------------------------------------------------------------------
-__global__ void k_count(BlockArgs A, int64_t *__restrict__ cntH, int64_t *__restrict__ cntS,
-                        unsigned long long *__restrict__ ref) {
+__global__ void k_csr_count(BlockArgs A, int64_t *__restrict__ cntH, int64_t *__restrict__ cntS,
+                            unsigned long long *__restrict__ stats) {
     int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    long long refH = 0, refS = 0;
+    long long refH = 0, refS = 0, totH = 0, totS = 0;
     if (row < A.n_rows) {
-        int4 rw = A.rows[row];
-        int n_a = rw.x, n_b = rw.y, c_r = rw.z;
+        const bs2e_config cf = A.cfg[row];
+        int n_a = (int)cf.n1, n_b = (int)cf.n2;
+        int c_r = A.lmap[cf.l1 * kMaxL + cf.l2];
         const int k = A.k;
         int64_t ch = 0, cs = 0;
         for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
@@ -162,15 +166,82 @@ __global__ void k_count(BlockArgs A, int64_t *__restrict__ cntH, int64_t *__rest
         }
         cntH[row] = ch;
         cntS[row] = cs;
+        totH = ch;
+        totS = cs;
     }
-    // block reduction of the reference counts
+    // warp reduction of the totals of both predicates
     for (int o = 16; o > 0; o >>= 1) {
         refH += __shfl_down_sync(0xffffffffu, refH, o);
         refS += __shfl_down_sync(0xffffffffu, refS, o);
+        totH += __shfl_down_sync(0xffffffffu, totH, o);
+        totS += __shfl_down_sync(0xffffffffu, totS, o);
     }
-    if ((threadIdx.x & 31) == 0 && (refH || refS)) {
-        atomicAdd(&ref[0], (unsigned long long)refH);
-        atomicAdd(&ref[1], (unsigned long long)refS);
+    if ((threadIdx.x & 31) == 0 && (refH || refS || totH || totS)) {
+        atomicAdd(&stats[1], (unsigned long long)refH);
+        atomicAdd(&stats[2], (unsigned long long)refS);
+        atomicAdd(&stats[3], (unsigned long long)totH);
+        atomicAdd(&stats[4], (unsigned long long)totS);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Device-side planning of a block from its configuration list.
+// stats[0] error bits: 1 = n or l out of range, 2 = not in basis order.
+// ---------------------------------------------------------------------------
+__global__ void k_cfg_equal(const bs2e_config *__restrict__ a, const bs2e_config *__restrict__ b,
+                            int64_t n, unsigned long long *__restrict__ stats) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bs2e_config x = a[i], y = b[i];
+        if (x.n1 != y.n1 || x.n2 != y.n2 || x.l1 != y.l1 || x.l2 != y.l2 || x.eqv != y.eqv)
+            atomicOr(&stats[6], 1ull);
+    }
+}
+
+// Rows where a new channel (l1, l2) starts, appended in any order.
+__global__ void k_chan_marks(const bs2e_config *__restrict__ cfg, int64_t n, int N,
+                             int4 *__restrict__ marks, int cap,
+                             unsigned long long *__restrict__ stats) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bs2e_config c = cfg[i];
+        if (c.n1 < 1 || c.n1 > N || c.n2 < 1 || c.n2 > N || c.l1 < 0 || c.l2 < 0 ||
+            c.l1 >= kMaxL || c.l2 >= kMaxL) {
+            atomicOr(&stats[0], 1ull);
+            continue;
+        }
+        bool start = (i == 0) || cfg[i - 1].l1 != c.l1 || cfg[i - 1].l2 != c.l2;
+        if (start) {
+            unsigned long long slot = atomicAdd(&stats[5], 1ull);
+            if (slot < (unsigned long long)cap) marks[slot] = make_int4((int)i, (int)c.l1, (int)c.l2, 0);
+        }
+    }
+}
+
+// Segment tables and basis-order checks: within a channel n1 ascends, and the
+// n2 of one (channel, n1) group are consecutive.
+__global__ void k_plan_seg(const bs2e_config *__restrict__ cfg, int64_t n, const int *__restrict__ lmap,
+                           int segS, int *__restrict__ seg_base, int *__restrict__ seg_lo,
+                           int *__restrict__ seg_hi, unsigned long long *__restrict__ stats) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const bs2e_config c = cfg[i];
+        if (c.l1 < 0 || c.l2 < 0 || c.l1 >= kMaxL || c.l2 >= kMaxL) continue;  // flagged already
+        const int ch = lmap[c.l1 * kMaxL + c.l2];
+        bool new_ch = (i == 0) || cfg[i - 1].l1 != c.l1 || cfg[i - 1].l2 != c.l2;
+        bool new_grp = new_ch || cfg[i - 1].n1 != c.n1;
+        if (!new_ch) {
+            const bs2e_config p = cfg[i - 1];
+            if (new_grp ? !(c.n1 > p.n1) : (c.n2 != p.n2 + 1)) atomicOr(&stats[0], 2ull);
+        }
+        bool last = (i == n - 1) || cfg[i + 1].l1 != c.l1 || cfg[i + 1].l2 != c.l2 ||
+                    cfg[i + 1].n1 != c.n1;
+        size_t s = (size_t)ch * segS + (size_t)c.n1;
+        if (new_grp) {
+            seg_base[s] = (int)i;
+            seg_lo[s] = (int)c.n2;
+        }
+        if (last) seg_hi[s] = (int)c.n2;
     }
 }
 
@@ -257,11 +328,14 @@ __global__ void k_scan_final(const int64_t *__restrict__ in, int64_t n,
 // ---------------------------------------------------------------------------
 struct FillArgs {
     BlockArgs B;
-    const int *tile_ab, *tile_ptr, *tile_rows;
     const double *R;
+    const float2 *Rf;  // mixed store (scaled FP32 pairs) and its per-(tile, k) exponents
+    const int *Rexp;
     int64_t tile;
     const double2 *Hb, *Sb;
+    const float4 *Hbf, *Sbf;  // the same bands as FP32 pairs (re hi, re lo, im hi, im lo)
     int s_real;
+    int ff_one_body;          // 1: mixed path may use Hbf/Sbf (S real, magnitudes in range)
     const int64_t *Hptr, *Sptr;  // 1-based CSR pointers of the block
     int64_t *Hidx, *Sidx;
     double2 *Hdat, *Sdat;
@@ -278,6 +352,12 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
 __device__ __forceinline__ double2 band(const double2 *M, int N, int k, int x, int y) {
     int d = y - x;
     if (d >= k || -d >= k) return make_double2(0.0, 0.0);
+    return M[(size_t)(x - 1) * (2 * k - 1) + (d + k - 1)];
+}
+
+__device__ __forceinline__ float4 bandf(const float4 *M, int k, int x, int y) {
+    int d = y - x;
+    if (d >= k || -d >= k) return make_float4(0.f, 0.f, 0.f, 0.f);
     return M[(size_t)(x - 1) * (2 * k - 1) + (d + k - 1)];
 }
 
@@ -333,23 +413,160 @@ __device__ bool stage_tile(const double *src, double *dst, uint32_t bytes, uint6
     return true;
 }
 
-__global__ void __launch_bounds__(128) k_fill(FillArgs F) {
+// ---- FP32-pair (double-float) arithmetic of the mixed path ----------------
+struct FF {
+    float s, c;
+};
+
+// acc += a * x for double-float a, x; the product error is captured exactly
+// with fmaf and the sum by TwoSum, so the pair keeps ~44 bits.
+__device__ __forceinline__ void ff_madd(FF &acc, float2 a, float2 x) {
+    float p = __fmul_rn(a.x, x.x);
+    float e = fmaf(a.x, x.x, -p);
+    e = fmaf(a.x, x.y, e);
+    e = fmaf(a.y, x.x, e);
+    float t = __fadd_rn(acc.s, p);
+    float bp = __fsub_rn(t, acc.s);
+    float err = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    acc.s = t;
+    acc.c = __fadd_rn(acc.c, __fadd_rn(err, e));
+}
+
+// 2^n as float for -126 <= n <= 127, 0 below.
+__device__ __forceinline__ float pow2f(int n) {
+    return n < -126 ? 0.0f : __int_as_float((127 + min(n, 127)) << 23);
+}
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    float s = __fadd_rn(a, b);
+    float bp = __fsub_rn(s, a);
+    float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+    return FF{s, e};
+}
+
+// Exact product a*b of two FP32 pairs up to the lo*lo term, unnormalised.
+__device__ __forceinline__ FF ff_mul(float2 a, float2 b) {
+    float p = __fmul_rn(a.x, b.x);
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return FF{p, e};
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF t = two_sum(a.s, b.s);
+    t.c = __fadd_rn(t.c, __fadd_rn(a.c, b.c));
+    return t;
+}
+
+__device__ __forceinline__ FF ff_neg_if(FF a, bool neg) {
+    return neg ? FF{-a.s, -a.c} : a;
+}
+
+// (s + c) * 2^shift rounded to double, assembled from the bit patterns with
+// integer arithmetic only: the pair is renormalised by TwoSum, both
+// significands are aligned in a 64-bit integer and rounded to 53 bits.  A
+// subnormal leading part (never met for in-range values) takes an FP64 path.
+__device__ __forceinline__ double ff_to_double(FF v, int shift) {
+    FF n = two_sum(v.s, v.c);
+    uint32_t us = __float_as_uint(n.s), uc = __float_as_uint(n.c);
+    int es = (int)((us >> 23) & 0xffu), ec = (int)((uc >> 23) & 0xffu);
+    if (es == 0) {
+        if ((us & 0x7fffffu) == 0) return 0.0;
+        return ((double)n.s + (double)n.c) * __longlong_as_double((long long)(1023 + shift) << 52);
+    }
+    long long M = (long long)(((uint64_t)((us & 0x7fffffu) | 0x800000u)) << 39);
+    if (ec != 0) {
+        long long mc = (long long)((uc & 0x7fffffu) | 0x800000u);
+        int sh = 39 - (es - ec);
+        long long add = sh >= 0 ? (mc << sh) : (sh > -24 ? (mc >> -sh) : 0);
+        M = ((us ^ uc) >> 31) ? M - add : M + add;
+    }
+    int p = 63 - __clzll(M);  // leading bit, 61 or 62
+    int drop = p - 52;
+    uint64_t um = (uint64_t)M;
+    uint64_t mant = um >> drop;
+    uint64_t rem = um & ((1ull << drop) - 1);
+    uint64_t half = 1ull << (drop - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) mant++;
+    if (mant >> 53) {
+        mant >>= 1;
+        p++;
+    }
+    int e2 = es - 189 + shift + p;  // exponent of the leading bit
+    uint64_t bits = ((uint64_t)(us >> 31) << 63) | ((uint64_t)(e2 + 1023) << 52) |
+                    (mant & ((1ull << 52) - 1));
+    return __longlong_as_double((long long)bits);
+}
+
+// a 2^Ea + b 2^Eb as one pair with exponent max(Ea, Eb).
+__device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bool has_b,
+                                      int &E) {
+    if (!has_a && !has_b) {
+        E = 0;
+        return FF{0.f, 0.f};
+    }
+    if (!has_b) {
+        E = Ea;
+        return a;
+    }
+    if (!has_a) {
+        E = Eb;
+        return b;
+    }
+    if (Ea < Eb) {
+        FF t = a;
+        a = b;
+        b = t;
+        int te = Ea;
+        Ea = Eb;
+        Eb = te;
+    }
+    float sc = pow2f(Eb - Ea);
+    E = Ea;
+    return ff_add(a, FF{__fmul_rn(b.s, sc), __fmul_rn(b.c, sc)});
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
+    __shared__ int sexp[kMaxK1];
+    __shared__ float2 sA[4][2][kMaxK1];
+    __shared__ int sKo[4][2][kMaxK1];
+    __shared__ int srow[kMaxCh], sch[kMaxCh], snrow;
     const BlockArgs &A = F.B;
-    const int t = blockIdx.x;
-    const int n_a = F.tile_ab[2 * t], n_b = F.tile_ab[2 * t + 1];
-    const double *src = F.R + (size_t)((n_a - 1) * A.N + (n_b - 1)) * F.tile;
+    const int n_a = blockIdx.x / A.N + 1, n_b = blockIdx.x % A.N + 1;
+    const size_t tix = (size_t)blockIdx.x;
+    // rows of this tile: one per channel whose (n1 = n_a) group holds n2 = n_b
+    if (threadIdx.x == 0) snrow = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < A.n_ch; c += blockDim.x) {
+        size_t s = (size_t)c * A.segS + n_a;
+        int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
+        if (base >= 0 && lo <= n_b && n_b <= hi) {
+            int slot = atomicAdd(&snrow, 1);
+            srow[slot] = base + (n_b - lo);
+            sch[slot] = c;
+        }
+    }
+    __syncthreads();
+    const int nrow = snrow;
+    if (nrow == 0) return;
+    const double *src = MIXED ? (const double *)(F.Rf + tix * F.tile) : F.R + tix * F.tile;
+    if (MIXED) {
+        for (int i = threadIdx.x; i < A.K1; i += blockDim.x) sexp[i] = F.Rexp[tix * A.K1 + i];
+    }
     if (!stage_tile(src, sR, (uint32_t)(F.tile * sizeof(double)), &bar, F.err)) return;
+    const float2 *sR2 = (const float2 *)sR;
 
     const int k = A.k, W = 2 * k - 1, W2 = W * W, K1 = A.K1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const unsigned FULL = 0xffffffffu;
-    for (int rr = F.tile_ptr[t] + warp; rr < F.tile_ptr[t + 1]; rr += nwarp) {
-        const int row = F.tile_rows[rr];
-        const int4 rw = A.rows[row];
-        const int c_r = rw.z;
-        const int l_a = rw.w >> 8, l_b = rw.w & 255;  // row channel (l1, l2)
+    for (int rr = warp; rr < nrow; rr += nwarp) {
+        const int row = srow[rr];
+        const int c_r = sch[rr];
+        const int l_a = A.chl[c_r] >> 8, l_b = A.chl[c_r] & 255;  // row channel (l1, l2)
         int64_t oH = F.Hptr[row] - 1, oS = F.Sptr[row] - 1;
         for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
             const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
@@ -365,6 +582,32 @@ __global__ void __launch_bounds__(128) k_fill(FillArgs F) {
             const int8_t *kx = kd + K1;
             const double *ad = A.pair_a + pbase;
             const double *ax = ad + K1;
+            int Ed = 0, Ex = 0;
+            if (MIXED) {
+                // scaled multipole weights of this channel pair for this tile
+                int ed = -100000, ex = -100000;
+                if (lane < pi.nd) ed = sexp[kd[lane]];
+                if (lane < pi.nx) ex = sexp[kx[lane]];
+                Ed = ed;
+                Ex = ex;
+                for (int o = 16; o > 0; o >>= 1) {
+                    Ed = max(Ed, __shfl_xor_sync(FULL, Ed, o));
+                    Ex = max(Ex, __shfl_xor_sync(FULL, Ex, o));
+                }
+                if (lane < pi.nd) {
+                    const float *af = A.pair_af + (pbase + lane) * 2;
+                    float sc = pow2f(ed - Ed);
+                    sA[warp][0][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
+                    sKo[warp][0][lane] = kd[lane] * W2;
+                }
+                if (lane < pi.nx) {
+                    const float *af = A.pair_af + (pbase + K1 + lane) * 2;
+                    float sc = pow2f(ex - Ex);
+                    sA[warp][1][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
+                    sKo[warp][1][lane] = kx[lane] * W2;
+                }
+                __syncwarp();
+            }
             for (int g0 = 0; g0 < ncand; g0 += 32) {
                 const int ci = g0 + lane;
                 Iv2 hs{0, 0, 0, 0}, ss{0, 0, 0, 0};
@@ -406,23 +649,90 @@ __global__ void __launch_bounds__(128) k_fill(FillArgs F) {
                             const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
                             const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
                             double re = 0.0, im = 0.0;
-                            if ((sup && dir_ok) || (supx && ex_ok)) {
-                                double res = 0.0;
-                                if (sup) {
-                                    const double *Rt = sR + (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
-                                    double r = 0.0;
-                                    for (int u = 0; u < pi.nd; ++u) r = fma(Rt[kd[u] * W2], ad[u], r);
-                                    res = res + r;
+                            const bool r12 = (sup && dir_ok) || (supx && ex_ok);
+                            const bool one = (sup && leq) || (supx && leqx);
+                            if (MIXED && F.ff_one_body) {
+                                // everything in FP32-pair arithmetic, one rounding to double
+                                FF v{0.f, 0.f};
+                                int Ev = 0;
+                                bool has = false;
+                                if (r12) {
+                                    const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
+                                    const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
+                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                    if (sup)
+                                        for (int u = 0; u < pi.nd; ++u)
+                                            ff_madd(fd, sA[warp][0][u], sR2[sKo[warp][0][u] + od]);
+                                    if (supx)
+                                        for (int u = 0; u < pi.nx; ++u)
+                                            ff_madd(fx, sA[warp][1][u], sR2[sKo[warp][1][u] + ox]);
+                                    v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                    has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
                                 }
-                                if (supx) {
-                                    const double *Rt = sR + (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
-                                    double r = 0.0;
-                                    for (int u = 0; u < pi.nx; ++u) r = fma(Rt[kx[u] * W2], ax[u], r);
-                                    res = res + r;
+                                FF hi_im{0.f, 0.f};
+                                if (one) {
+                                    // H_1p_neq (mat_els.f90:697-715) with real S
+                                    const float4 *Ha = F.Hbf + (size_t)l_a * A.N * W;
+                                    const float4 *Hbb = F.Hbf + (size_t)l_b * A.N * W;
+                                    FF hr{0.f, 0.f};
+                                    if (leq) {
+                                        float4 h1 = bandf(Ha, k, n_a, r_nc), s1 = bandf(F.Sbf, k, n_b, n_d);
+                                        float4 h2 = bandf(Hbb, k, n_b, n_d), s2 = bandf(F.Sbf, k, n_a, r_nc);
+                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                        hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                    ff_mul(make_float2(h2.x, h2.y), s2r));
+                                        hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
+                                    }
+                                    if (leqx) {
+                                        float4 h1 = bandf(Ha, k, n_a, n_d), s1 = bandf(F.Sbf, k, n_b, r_nc);
+                                        float4 h2 = bandf(Hbb, k, n_b, r_nc), s2 = bandf(F.Sbf, k, n_a, n_d);
+                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                        bool ng = pi.sgn < 0.0;
+                                        FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                       ff_mul(make_float2(h2.x, h2.y), s2r));
+                                        FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
+                                        hr = ff_add(hr, ff_neg_if(xr, ng));
+                                        hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
+                                    }
+                                    v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
+                                    has = true;
                                 }
-                                re = res;
+                                re = has ? ff_to_double(v, Ev - kRkBias) : 0.0;
+                                im = one ? ff_to_double(hi_im, 0) : 0.0;
+                            } else if (r12) {
+                                const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
+                                const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
+                                if (MIXED) {
+                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                    if (sup)
+                                        for (int u = 0; u < pi.nd; ++u)
+                                            ff_madd(fd, sA[warp][0][u], sR2[sKo[warp][0][u] + od]);
+                                    if (supx)
+                                        for (int u = 0; u < pi.nx; ++u)
+                                            ff_madd(fx, sA[warp][1][u], sR2[sKo[warp][1][u] + ox]);
+                                    int Ev;
+                                    FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                    re = ff_to_double(v, Ev - kRkBias);
+                                } else {
+                                    double res = 0.0;
+                                    if (sup) {
+                                        const double *Rt = sR + od;
+                                        double r = 0.0;
+                                        for (int u = 0; u < pi.nd; ++u) r = fma(Rt[kd[u] * W2], ad[u], r);
+                                        res = res + r;
+                                    }
+                                    if (supx) {
+                                        const double *Rt = sR + ox;
+                                        double r = 0.0;
+                                        for (int u = 0; u < pi.nx; ++u) r = fma(Rt[kx[u] * W2], ax[u], r);
+                                        res = res + r;
+                                    }
+                                    re = res;
+                                }
                             }
-                            if ((sup && leq) || (supx && leqx)) {
+                            if (one && !(MIXED && F.ff_one_body)) {
                                 // H_1p_neq (mat_els.f90:697-715)
                                 const int N = A.N;
                                 const double2 *Ha = F.Hb + (size_t)l_a * N * W;
@@ -481,11 +791,25 @@ __global__ void __launch_bounds__(128) k_fill(FillArgs F) {
                             // S_mat_neq (mat_els.f90:664-678)
                             const int N = A.N;
                             double2 s1 = make_double2(0.0, 0.0);
-                            if (leq) s1 = cadd(s1, cmul(band(F.Sb, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d)));
-                            if (leqx) {
-                                double2 a = band(F.Sb, N, k, n_a, n_d);
-                                a = make_double2(a.x * pi.sgn, a.y * pi.sgn);
-                                s1 = cadd(s1, cmul(a, band(F.Sb, N, k, n_b, r_nc)));
+                            if (MIXED && F.ff_one_body) {
+                                FF t{0.f, 0.f};
+                                if (leq) {
+                                    float4 a = bandf(F.Sbf, k, n_a, r_nc), b = bandf(F.Sbf, k, n_b, n_d);
+                                    t = ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y));
+                                }
+                                if (leqx) {
+                                    float4 a = bandf(F.Sbf, k, n_a, n_d), b = bandf(F.Sbf, k, n_b, r_nc);
+                                    t = ff_add(t, ff_neg_if(ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y)),
+                                                            pi.sgn < 0.0));
+                                }
+                                s1 = make_double2(ff_to_double(t, 0), 0.0);
+                            } else {
+                                if (leq) s1 = cadd(s1, cmul(band(F.Sb, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d)));
+                                if (leqx) {
+                                    double2 a = band(F.Sb, N, k, n_a, n_d);
+                                    a = make_double2(a.x * pi.sgn, a.y * pi.sgn);
+                                    s1 = cadd(s1, cmul(a, band(F.Sb, N, k, n_b, r_nc)));
+                                }
                             }
                             F.Sidx[oS + e] = (int64_t)j + 1;
                             F.Sdat[oS + e] = s1;
@@ -502,15 +826,19 @@ __global__ void __launch_bounds__(128) k_fill(FillArgs F) {
 
 static BlockArgs block_args(bs2e_handle *h) {
     BlockArgs A;
-    A.rows = h->blk.rows;
+    const DevBlock &B = h->blk;
     int S = h->g.N + 2;
+    A.cfg = B.cfg;
+    A.lmap = B.lmap;
+    A.chl = B.chl;
     A.segS = S;
-    A.seg_base = h->blk.seg;
-    A.seg_lo = h->blk.seg + (size_t)h->plan.n_ch * S;
-    A.seg_hi = h->blk.seg + (size_t)2 * h->plan.n_ch * S;
-    A.pairs = h->blk.pairs;
-    A.pair_k = h->blk.pair_k;
-    A.pair_a = h->blk.pair_a;
+    A.seg_base = B.seg;
+    A.seg_lo = B.seg + (size_t)h->plan.n_ch * S;
+    A.seg_hi = B.seg + (size_t)2 * h->plan.n_ch * S;
+    A.pairs = B.pairs;
+    A.pair_k = B.pair_k;
+    A.pair_a = B.pair_a;
+    A.pair_af = B.pair_af;
     A.n_ch = h->plan.n_ch;
     A.N = h->g.N;
     A.k = h->g.k;
@@ -520,13 +848,41 @@ static BlockArgs block_args(bs2e_handle *h) {
     return A;
 }
 
+static inline unsigned grid_rows(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    if (g > (int64_t)152 * 32) g = (int64_t)152 * 32;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+void launch_cfg_equal(bs2e_handle *h, int64_t n) {
+    if (n <= 0) return;
+    k_cfg_equal<<<grid_rows(n), 256, 0, h->stream>>>(h->blk.cfg_new, h->blk.cfg, n, h->blk.stats);
+    h->launches++;
+}
+
+void launch_chan_marks(bs2e_handle *h, int64_t n) {
+    if (n <= 0) return;
+    k_chan_marks<<<grid_rows(n), 256, 0, h->stream>>>(h->blk.cfg_new, n, h->g.N, h->blk.marks,
+                                                       kMaxCh + 1, h->blk.stats);
+    h->launches++;
+}
+
+void launch_plan_seg(bs2e_handle *h, int64_t n) {
+    if (n <= 0) return;
+    BlockArgs A = block_args(h);
+    k_plan_seg<<<grid_rows(n), 256, 0, h->stream>>>(h->blk.cfg_new, n, A.lmap, A.segS,
+                                                     (int *)A.seg_base, (int *)A.seg_lo,
+                                                     (int *)A.seg_hi, h->blk.stats);
+    h->launches++;
+}
+
 void launch_block_count(bs2e_handle *h) {
     BlockArgs A = block_args(h);
+    A.cfg = h->blk.cfg_new;
     int64_t n = h->plan.n_config;
-    unsigned long long *ref = (unsigned long long *)h->blk.scan_tmp;  // first two words
-    cudaMemsetAsync(ref, 0, 2 * sizeof(unsigned long long), h->stream);
     if (n > 0) {
-        k_count<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(A, h->blk.cntH, h->blk.cntS, ref);
+        k_csr_count<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(A, h->blk.cntH, h->blk.cntS,
+                                                                     h->blk.stats);
         h->launches++;
     }
 }
@@ -542,7 +898,7 @@ static void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part
 
 void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr) {
     int64_t n = h->plan.n_config;
-    int64_t *part = h->blk.scan_tmp + 2;
+    int64_t *part = h->blk.scan_tmp;
     scan_one(h, h->blk.cntH, n, part, d_Hptr);
     scan_one(h, h->blk.cntS, n, part, d_Sptr);
 }
@@ -553,14 +909,16 @@ void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_S
                        int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx, double2 *d_Sdat) {
     FillArgs F;
     F.B = block_args(h);
-    F.tile_ab = h->blk.tile_ab;
-    F.tile_ptr = h->blk.tile_ptr;
-    F.tile_rows = h->blk.tile_rows;
     F.R = h->d_R;
+    F.Rf = h->d_Rf;
+    F.Rexp = h->d_Rexp;
     F.tile = h->g.tile;
     F.Hb = h->d_Hb;
     F.Sb = h->d_Sb;
+    F.Hbf = h->d_Hbf;
+    F.Sbf = h->d_Sbf;
     F.s_real = h->s_real ? 1 : 0;
+    F.ff_one_body = h->ff_one_body ? 1 : 0;
     F.Hptr = d_Hptr;
     F.Sptr = d_Sptr;
     F.Hidx = d_Hidx;
@@ -569,9 +927,15 @@ void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_S
     F.Sdat = d_Sdat;
     F.err = h->d_err;
     size_t smem = fill_smem(h->g);
-    cudaFuncSetAttribute(k_fill, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (h->blk.n_tiles > 0) {
-        k_fill<<<(unsigned)h->blk.n_tiles, 128, smem, h->stream>>>(F);
+    if (h->plan.n_config > 0) {
+        const unsigned tiles = (unsigned)((int64_t)h->g.N * h->g.N);
+        if (h->precision == BS2E_PREC_MIXED) {
+            cudaFuncSetAttribute(k_csr_fill<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_csr_fill<true><<<tiles, 128, smem, h->stream>>>(F);
+        } else {
+            cudaFuncSetAttribute(k_csr_fill<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_csr_fill<false><<<tiles, 128, smem, h->stream>>>(F);
+        }
         h->launches++;
     }
 }

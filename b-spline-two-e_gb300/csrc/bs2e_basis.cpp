@@ -57,83 +57,14 @@ static bool consistent(int64_t l1, int64_t l2, int64_t L, int64_t parity_odd, bo
     return par == (parity_odd != 0);
 }
 
-bs2e_status build_plan(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
-                       int64_t full, const Radial &g, BlockPlan &P, std::string &err) {
-    P = BlockPlan();
-    P.n_config = n_config;
-    P.L = L;
-    P.spin = spin;
-    P.full = full;
-    const int N = g.N;
-    if (n_config < 0 || n_config > (int64_t)1 << 30) {
-        err = "n_config out of range";
-        return BS2E_ERR_ARG;
-    }
-    P.row_n1.resize(n_config);
-    P.row_n2.resize(n_config);
-    P.row_ch.resize(n_config);
-    // channels in order of appearance, each one contiguous
-    int cur = -1;
-    for (int64_t i = 0; i < n_config; ++i) {
-        const bs2e_config &c = cf[i];
-        if (c.n1 < 1 || c.n1 > N || c.n2 < 1 || c.n2 > N || c.l1 < 0 || c.l2 < 0 || c.l1 > 63 ||
-            c.l2 > 63) {
-            err = "configuration " + std::to_string(i + 1) + " has n or l out of range";
-            return BS2E_ERR_ARG;
-        }
-        if (cur < 0 || P.ch_l1[cur] != c.l1 || P.ch_l2[cur] != c.l2) {
-            for (int q = 0; q < (int)P.ch_l1.size(); ++q)
-                if (P.ch_l1[q] == c.l1 && P.ch_l2[q] == c.l2) {
-                    err = "channel (" + std::to_string(c.l1) + "," + std::to_string(c.l2) +
-                          ") is not contiguous in the configuration list";
-                    return BS2E_ERR_ORDER;
-                }
-            P.ch_l1.push_back((int)c.l1);
-            P.ch_l2.push_back((int)c.l2);
-            cur = (int)P.ch_l1.size() - 1;
-        }
-        P.row_n1[i] = (int)c.n1;
-        P.row_n2[i] = (int)c.n2;
-        P.row_ch[i] = cur;
-    }
-    P.n_ch = (int)P.ch_l1.size();
-    const int S = N + 2;
-    P.seg_base.assign((size_t)P.n_ch * S, -1);
-    P.seg_lo.assign((size_t)P.n_ch * S, 1);
-    P.seg_hi.assign((size_t)P.n_ch * S, 0);
-    for (int64_t i = 0; i < n_config;) {
-        int ch = P.row_ch[i], n1 = P.row_n1[i];
-        int64_t j = i;
-        while (j < n_config && P.row_ch[j] == ch && P.row_n1[j] == n1) {
-            if (j > i && P.row_n2[j] != P.row_n2[j - 1] + 1) {
-                err = "n2 values of one (channel, n1) group are not consecutive at configuration " +
-                      std::to_string(j + 1);
-                return BS2E_ERR_ORDER;
-            }
-            ++j;
-        }
-        size_t s = (size_t)ch * S + n1;
-        if (P.seg_base[s] >= 0) {
-            err = "n1 group repeated within a channel at configuration " + std::to_string(i + 1);
-            return BS2E_ERR_ORDER;
-        }
-        if (i > 0 && P.row_ch[i - 1] == ch && P.row_n1[i - 1] > n1) {
-            err = "n1 not ascending within a channel at configuration " + std::to_string(i + 1);
-            return BS2E_ERR_ORDER;
-        }
-        P.seg_base[s] = (int)i;
-        P.seg_lo[s] = P.row_n2[i];
-        P.seg_hi[s] = P.row_n2[j - 1];
-        i = j;
-    }
-    // channel-pair couplings
-    const int K1 = g.K1;
+void plan_channels(BlockPlan &P, int K1) {
     const int nc = P.n_ch;
+    const int64_t L = P.L;
     P.pairs.assign((size_t)nc * nc, PairInfo{});
     P.pair_k.assign((size_t)nc * nc * 2 * K1, 0);
     P.pair_a.assign((size_t)nc * nc * 2 * K1, 0.0);
     P.pair_af.assign((size_t)nc * nc * 2 * K1 * 2, 0.0f);
-    const double exsign = spin ? -1.0 : 1.0;
+    const double exsign = P.spin ? -1.0 : 1.0;
     for (int r = 0; r < nc; ++r)
         for (int c = 0; c < nc; ++c) {
             int la = P.ch_l1[r], lb = P.ch_l2[r], lc = P.ch_l1[c], ld = P.ch_l2[c];
@@ -172,27 +103,6 @@ bs2e_status build_plan(const bs2e_config *cf, int64_t n_config, int64_t L, int64
             pi.nx = nx;
             pi.sgn = sgn;
         }
-    // tiles: distinct (n_a, n_b) in a-major order with their rows
-    std::vector<int> cnt((size_t)N * N, 0);
-    for (int64_t i = 0; i < n_config; ++i) cnt[(size_t)(P.row_n1[i] - 1) * N + (P.row_n2[i] - 1)]++;
-    std::vector<int> tid((size_t)N * N, -1);
-    P.tile_ptr.push_back(0);
-    for (int a = 0; a < N; ++a)
-        for (int b = 0; b < N; ++b) {
-            size_t s = (size_t)a * N + b;
-            if (!cnt[s]) continue;
-            tid[s] = (int)P.tile_a.size();
-            P.tile_a.push_back(a + 1);
-            P.tile_b.push_back(b + 1);
-            P.tile_ptr.push_back(P.tile_ptr.back() + cnt[s]);
-        }
-    P.tile_rows.assign(n_config, 0);
-    std::vector<int> fillp(P.tile_ptr.begin(), P.tile_ptr.end() - 1);
-    for (int64_t i = 0; i < n_config; ++i) {
-        int t = tid[(size_t)(P.row_n1[i] - 1) * N + (P.row_n2[i] - 1)];
-        P.tile_rows[fillp[t]++] = (int)i;
-    }
-    return BS2E_OK;
 }
 
 }  // namespace bs2e

@@ -75,30 +75,34 @@ int splines_on(const Radial &g, int iv) {
 }
 
 void free_block(DevBlock &b) {
-    dfree(b.rows);
+    dfree(b.cfg);
+    dfree(b.cfg_new);
+    dfree(b.marks);
+    dfree(b.lmap);
+    dfree(b.chl);
     dfree(b.seg);
     dfree(b.pairs);
     dfree(b.pair_k);
     dfree(b.pair_a);
     dfree(b.pair_af);
-    dfree(b.tile_ab);
-    dfree(b.tile_ptr);
-    dfree(b.tile_rows);
     dfree(b.cntH);
     dfree(b.cntS);
     dfree(b.scan_tmp);
-    b.n_tiles = 0;
+    dfree(b.stats);
+    b.cfg_cap = b.cfg_new_cap = b.seg_cap = b.pair_cap = b.cnt_cap = b.scan_cap = 0;
     b.nnzH = b.nnzS = -1;
     b.valid = false;
 }
 
+// Grows a device buffer to hold at least n elements (contents not kept).
 template <class T>
-bs2e_status upload(bs2e_handle *h, T **dst, const std::vector<T> &src) {
-    CU(dalloc(dst, src.size()));
-    if (!src.empty())
-        CU(cudaMemcpyAsync(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice,
-                           h->stream));
-    return BS2E_OK;
+cudaError_t grow(T **p, int64_t &cap, int64_t n) {
+    if (n <= cap && *p) return cudaSuccess;
+    dfree(*p);
+    int64_t c = std::max<int64_t>(n, 1);
+    cudaError_t e = dalloc(p, (size_t)c);
+    cap = (e == cudaSuccess) ? c : 0;
+    return e;
 }
 
 #define TRY(x)                              \
@@ -107,88 +111,141 @@ bs2e_status upload(bs2e_handle *h, T **dst, const std::vector<T> &src) {
         if (s_ != BS2E_OK) return s_;       \
     } while (0)
 
-// Builds, uploads and counts one block unless it is the cached one.
+// Uploads the configuration list and, unless it is the block counted last,
+// plans it on the device (channels, segment tables, order checks) and counts
+// its non-zeros with both the construct and the count_nnz predicates.
 bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_config, int64_t L,
                            int64_t spin, int64_t full) {
     if (!cf && n_config > 0) return fail(h, BS2E_ERR_ARG, "configs is NULL");
     if (L < 0 || (spin != 0 && spin != 1) || (full != 0 && full != 1))
         return fail(h, BS2E_ERR_ARG, "L, spin or full out of range");
-    {
-        const DevBlock &b = h->blk;
-        if (b.valid && b.L == L && b.spin == spin && b.full == full &&
-            (int64_t)b.cfg.size() == n_config &&
-            (n_config == 0 || memcmp(b.cfg.data(), cf, sizeof(bs2e_config) * n_config) == 0))
-            return BS2E_OK;
-    }
-    free_block(h->blk);
-    std::string err;
-    bs2e_status st = build_plan(cf, n_config, L, spin, full, h->g, h->plan, err);
-    if (st != BS2E_OK) return fail(h, st, err);
-    BlockPlan &P = h->plan;
+    if (n_config > ((int64_t)1 << 31) - 2) return fail(h, BS2E_ERR_ARG, "n_config too large");
     DevBlock &B = h->blk;
-    for (int c = 0; c < P.n_ch; ++c)
-        if (P.ch_l1[c] > 255 || P.ch_l2[c] > 255) return fail(h, BS2E_ERR_ARG, "l above 255");
-    std::vector<int4> rows((size_t)n_config);
-    for (int64_t i = 0; i < n_config; ++i) {
-        int c = P.row_ch[i];
-        rows[i] = make_int4(P.row_n1[i], P.row_n2[i], c, (P.ch_l1[c] << 8) | P.ch_l2[c]);
+    const Radial &g = h->g;
+    if (!B.stats) CU(dalloc(&B.stats, 8));
+    if (!B.marks) CU(dalloc(&B.marks, kMaxCh + 1));
+    if (!B.lmap) CU(dalloc(&B.lmap, (size_t)kMaxL * kMaxL));
+    if (!B.chl) CU(dalloc(&B.chl, kMaxCh));
+    CU(grow(&B.cfg_new, B.cfg_new_cap, n_config));
+    if (n_config > 0)
+        CU(cudaMemcpyAsync(B.cfg_new, cf, sizeof(bs2e_config) * n_config, cudaMemcpyHostToDevice,
+                           h->stream));
+    CU(cudaMemsetAsync(B.stats, 0, 8 * sizeof(unsigned long long), h->stream));
+    unsigned long long st[8];
+    if (B.valid && B.L == L && B.spin == spin && B.full == full && B.n == n_config) {
+        launch_cfg_equal(h, n_config);
+        CU(cudaMemcpyAsync(st, B.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+        TRY(sync_check(h, "block compare"));
+        if (st[6] == 0) return BS2E_OK;  // same block as the last count
+        CU(cudaMemsetAsync(B.stats, 0, 8 * sizeof(unsigned long long), h->stream));
     }
-    std::vector<int> seg;
-    seg.reserve(P.seg_base.size() * 3);
-    seg.insert(seg.end(), P.seg_base.begin(), P.seg_base.end());
-    seg.insert(seg.end(), P.seg_lo.begin(), P.seg_lo.end());
-    seg.insert(seg.end(), P.seg_hi.begin(), P.seg_hi.end());
-    std::vector<int> tab(P.tile_a.size() * 2);
-    for (size_t t = 0; t < P.tile_a.size(); ++t) {
-        tab[2 * t] = P.tile_a[t];
-        tab[2 * t + 1] = P.tile_b[t];
+    B.valid = false;
+    BlockPlan &P = h->plan;
+    P = BlockPlan();
+    P.n_config = n_config;
+    P.L = L;
+    P.spin = spin;
+    P.full = full;
+    // channels: starts found on the device, ordered on the host
+    std::vector<int4> marks(kMaxCh + 1);
+    launch_chan_marks(h, n_config);
+    CU(cudaMemcpyAsync(st, B.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(marks.data(), B.marks, sizeof(int4) * marks.size(), cudaMemcpyDeviceToHost,
+                       h->stream));
+    TRY(sync_check(h, "block plan"));
+    if (st[0] & 1ull) return fail(h, BS2E_ERR_ARG, "a configuration has n or l out of range");
+    if (st[5] > (unsigned long long)kMaxCh)
+        return fail(h, BS2E_ERR_ARG, "more than 256 channel runs in one block");
+    marks.resize((size_t)st[5]);
+    std::sort(marks.begin(), marks.end(), [](const int4 &a, const int4 &b) { return a.x < b.x; });
+    std::vector<int> lmap((size_t)kMaxL * kMaxL, -1), chl;
+    for (const int4 &m : marks) {
+        int &slot = lmap[(size_t)m.y * kMaxL + m.z];
+        if (slot >= 0)
+            return fail(h, BS2E_ERR_ORDER, "channel (" + std::to_string(m.y) + "," +
+                                               std::to_string(m.z) +
+                                               ") is not contiguous in the configuration list");
+        slot = P.n_ch++;
+        P.ch_l1.push_back(m.y);
+        P.ch_l2.push_back(m.z);
+        P.ch_start.push_back(m.x);
+        chl.push_back((m.y << 8) | m.z);
     }
-    TRY(upload(h, &B.rows, rows));
-    TRY(upload(h, &B.seg, seg));
-    TRY(upload(h, &B.pairs, P.pairs));
-    TRY(upload(h, &B.pair_k, P.pair_k));
-    TRY(upload(h, &B.pair_a, P.pair_a));
-    TRY(upload(h, &B.pair_af, P.pair_af));
-    TRY(upload(h, &B.tile_ab, tab));
-    TRY(upload(h, &B.tile_ptr, P.tile_ptr));
-    TRY(upload(h, &B.tile_rows, P.tile_rows));
-    B.n_tiles = (int64_t)P.tile_a.size();
-    CU(dalloc(&B.cntH, (size_t)n_config));
-    CU(dalloc(&B.cntS, (size_t)n_config));
-    int64_t nparts = (n_config + 4095) / 4096 + 2;
-    CU(dalloc(&B.scan_tmp, (size_t)(nparts + 4)));
+    plan_channels(P, g.K1);
+    const int S = g.N + 2;
+    const int64_t nseg = (int64_t)P.n_ch * S;
+    CU(grow(&B.seg, B.seg_cap, 3 * nseg));
+    const int64_t npair = (int64_t)P.n_ch * P.n_ch;
+    if (npair * 2 * g.K1 > B.pair_cap || !B.pairs) {
+        dfree(B.pairs);
+        dfree(B.pair_k);
+        dfree(B.pair_a);
+        dfree(B.pair_af);
+        int64_t c = std::max<int64_t>(npair, 1);
+        CU(dalloc(&B.pairs, (size_t)c));
+        CU(dalloc(&B.pair_k, (size_t)c * 2 * g.K1));
+        CU(dalloc(&B.pair_a, (size_t)c * 2 * g.K1));
+        CU(dalloc(&B.pair_af, (size_t)c * 2 * g.K1 * 2));
+        B.pair_cap = c * 2 * g.K1;
+    }
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream)
+                     : cudaSuccess;
+    };
+    CU(up(B.lmap, lmap.data(), sizeof(int) * lmap.size()));
+    CU(up(B.chl, chl.data(), sizeof(int) * chl.size()));
+    CU(up(B.pairs, P.pairs.data(), sizeof(PairInfo) * P.pairs.size()));
+    CU(up(B.pair_k, P.pair_k.data(), P.pair_k.size()));
+    CU(up(B.pair_a, P.pair_a.data(), sizeof(double) * P.pair_a.size()));
+    CU(up(B.pair_af, P.pair_af.data(), sizeof(float) * P.pair_af.size()));
+    CU(cudaMemsetAsync(B.seg, 0xff, sizeof(int) * nseg, h->stream));              // base = -1
+    CU(cudaMemsetAsync(B.seg + nseg, 0x7f, sizeof(int) * nseg, h->stream));       // lo = big
+    CU(cudaMemsetAsync(B.seg + 2 * nseg, 0x00, sizeof(int) * nseg, h->stream));   // hi = 0
+    launch_plan_seg(h, n_config);
+    CU(grow(&B.cntH, B.cnt_cap, n_config));
+    int64_t cap2 = B.cnt_cap;
+    CU(grow(&B.cntS, cap2, n_config));
+    CU(grow(&B.scan_tmp, B.scan_cap, (n_config + 4095) / 4096 + 4));
     launch_block_count(h);
-    // totals of the construct predicate, and the count_nnz predicate in scan_tmp[0..1]
-    std::vector<int64_t> ch((size_t)n_config), cs((size_t)n_config);
-    unsigned long long ref[2] = {0, 0};
-    if (n_config > 0) {
-        CU(cudaMemcpyAsync(ch.data(), B.cntH, sizeof(int64_t) * n_config, cudaMemcpyDeviceToHost,
-                           h->stream));
-        CU(cudaMemcpyAsync(cs.data(), B.cntS, sizeof(int64_t) * n_config, cudaMemcpyDeviceToHost,
-                           h->stream));
-    }
-    CU(cudaMemcpyAsync(ref, B.scan_tmp, sizeof(ref), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(st, B.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync_check(h, "block count"));
-    int64_t th = 0, ts = 0;
-    for (int64_t i = 0; i < n_config; ++i) {
-        th += ch[i];
-        ts += cs[i];
-    }
+    if (st[0] & 2ull)
+        return fail(h, BS2E_ERR_ORDER, "configurations are not in basis order (n1 ascending, "
+                                       "n2 consecutive within each (channel, n1) group)");
+    const int64_t th = (int64_t)st[3], ts = (int64_t)st[4];
     B.nnzH = th;
     B.nnzS = ts;
-    if ((int64_t)ref[0] != th || (int64_t)ref[1] != ts) {
+    if ((int64_t)st[1] != th || (int64_t)st[2] != ts) {
         char buf[256];
         snprintf(buf, sizeof buf,
                  "count_nnz contract broken for this block: construct gives nnz_H=%lld nnz_S=%lld, "
                  "count_nnz gives %lld %lld",
-                 (long long)th, (long long)ts, (long long)ref[0], (long long)ref[1]);
+                 (long long)th, (long long)ts, (long long)st[1], (long long)st[2]);
         return fail(h, BS2E_ERR_COUNT, buf);
     }
-    B.cfg.assign(cf, cf + n_config);
+    std::swap(B.cfg, B.cfg_new);
+    std::swap(B.cfg_cap, B.cfg_new_cap);
     B.L = L;
     B.spin = spin;
     B.full = full;
+    B.n = n_config;
     B.valid = true;
+    return BS2E_OK;
+}
+
+// Builds the FP32-pair copies of the one-body bands and decides whether the
+// mixed assembly may use them (S real and every magnitude in range).
+bs2e_status finish_one_body(bs2e_handle *h) {
+    const Radial &g = h->g;
+    dfree(h->d_Hbf);
+    dfree(h->d_Sbf);
+    CU(dalloc(&h->d_Hbf, (size_t)h->n_l * g.N * g.W));
+    CU(dalloc(&h->d_Sbf, (size_t)g.N * g.W));
+    launch_band_split(h);
+    int flag = 0;
+    CU(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "one-body split"));
+    h->ff_one_body = h->s_real && flag == 0;
     return BS2E_OK;
 }
 
@@ -255,12 +312,14 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
     bad(dalloc(&h->d_glw, q));
     bad(dalloc(&h->d_tab_r, niv * q));
     bad(dalloc(&h->d_tab_B, niv * q * kk));
+    bad(dalloc(&h->d_tab_D2, niv * q * kk));
     bad(dalloc(&h->d_tab_ri, niv * q * q));
     bad(dalloc(&h->d_tab_Bi, niv * q * q * kk));
     bad(dalloc(&h->d_mom, niv * K1 * 2 * kk * kk));
     bad(dalloc(&h->d_dint, niv * K1 * kk * kk * kk * kk));
     bad(dalloc(&h->d_tot, (size_t)2 * K1 * g.N * g.W));
     bad(dalloc(&h->d_err, 1));
+    bad(dalloc(&h->d_flag, 1));
     if (st == BS2E_OK) {
         bad(cudaMemcpy(h->d_knots, knots, sizeof(double) * n_knots, cudaMemcpyHostToDevice));
         bad(cudaMemcpy(h->d_glx, h->glx.data(), sizeof(double) * q, cudaMemcpyHostToDevice));
@@ -289,6 +348,7 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_glw);
         dfree(h->d_tab_r);
         dfree(h->d_tab_B);
+        dfree(h->d_tab_D2);
         dfree(h->d_tab_ri);
         dfree(h->d_tab_Bi);
         dfree(h->d_mom);
@@ -298,6 +358,9 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_Rf);
         dfree(h->d_Rexp);
         dfree(h->d_err);
+        dfree(h->d_flag);
+        dfree(h->d_Hbf);
+        dfree(h->d_Sbf);
         dfree(h->d_Hb);
         dfree(h->d_Sb);
         if (h->stream) cudaStreamDestroy(h->stream);
@@ -419,7 +482,12 @@ BS2E_API bs2e_status bs2e_rk(bs2e_handle *h, int64_t k_first, int64_t k_count) {
     if (!h->slater_done) return fail(h, BS2E_ERR_STATE, "bs2e_slater has not run");
     if (k_first < 0 || k_count < 1 || k_first + k_count > g.K1)
         return fail(h, BS2E_ERR_ARG, "multipole range out of bounds");
-    if (!h->d_R) CU(dalloc(&h->d_R, (size_t)g.N * g.N * g.tile));
+    if (h->precision == BS2E_PREC_MIXED) {
+        if (!h->d_Rf) CU(dalloc(&h->d_Rf, (size_t)g.N * g.N * g.tile));
+        if (!h->d_Rexp) CU(dalloc(&h->d_Rexp, (size_t)g.N * g.N * g.K1));
+    } else if (!h->d_R) {
+        CU(dalloc(&h->d_R, (size_t)g.N * g.N * g.tile));
+    }
     launch_rk_fill(h, (int)k_first, (int)k_count);
     TRY(sync_check(h, "rk"));
     for (int64_t kk = k_first; kk < k_first + k_count; ++kk) h->rk_done[kk] = 1;
@@ -430,7 +498,7 @@ BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t 
                                        double *vals) {
     if (!h || n < 0 || (n > 0 && (!keys || !vals))) return BS2E_ERR_ARG;
     Guard G(h);
-    if (!h->d_R) return fail(h, BS2E_ERR_STATE, "bs2e_rk has not run");
+    if (!h->d_R && !h->d_Rf) return fail(h, BS2E_ERR_STATE, "bs2e_rk has not run");
     if (n == 0) return BS2E_OK;
     int64_t *dk = nullptr;
     double *dv = nullptr;
@@ -485,7 +553,7 @@ BS2E_API bs2e_status bs2e_set_one_body(bs2e_handle *h, const double *H1p, int64_
     h->n_l = n_l;
     h->s_real = sreal;
     h->have_one_body = true;
-    return BS2E_OK;
+    return finish_one_body(h);
 }
 
 BS2E_API bs2e_status bs2e_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order,
@@ -494,6 +562,7 @@ BS2E_API bs2e_status bs2e_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64
     if (!h || n_l < 1 || n_l > 32 || cap_order < 0) return BS2E_ERR_ARG;
     Guard G(h);
     const Radial &g = h->g;
+    if (!h->slater_done) return fail(h, BS2E_ERR_STATE, "bs2e_slater has not run (tabulation)");
     const int N = g.N, W = g.W, k = g.k;
     dfree(h->d_Hb);
     dfree(h->d_Sb);
@@ -504,6 +573,7 @@ BS2E_API bs2e_status bs2e_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64
     h->n_l = n_l;
     h->s_real = true;
     h->have_one_body = true;
+    TRY(finish_one_body(h));
     if (H1p || S) {
         std::vector<double2> Hb((size_t)n_l * N * W), Sb((size_t)N * W);
         CU(cudaMemcpy(Hb.data(), h->d_Hb, Hb.size() * sizeof(double2), cudaMemcpyDeviceToHost));

@@ -4,6 +4,7 @@
 // K1 = max_k+1, q = k_GL points per interval, n_iv breakpoint intervals):
 //   tab_r   [n_iv][q]           outer quadrature radii of each interval
 //   tab_B   [n_iv][q][k]        values of the k splines non-zero on the interval
+//   tab_D2  [n_iv][q][k]        their second derivatives (one-body kinetic term)
 //   tab_ri  [n_iv][q][q]        inner radii on [t_iv, r_P] for every outer point P
 //   tab_Bi  [n_iv][q][q][k]     spline values at the inner radii
 //   mom     [n_iv][K1][2][k][k] per-interval moments (0: int B B r^k, 1: int B B r^-(k+1))
@@ -28,6 +29,7 @@ namespace bs2e {
 constexpr int kMaxOrder = 16;  // B-spline order limit (the reference allows 20 in BVALUE_D)
 constexpr int kMaxGL = 32;     // Gauss-Legendre points per interval
 constexpr int kMaxK1 = 32;     // multipoles 0..31
+constexpr int kRkBias = 96;    // mixed R^k store: a slice maximum is scaled to [2^96, 2^97)
 
 // Per (row channel, column channel) coupling of one symmetry block.
 struct PairInfo {
@@ -37,42 +39,46 @@ struct PairInfo {
     double sgn;      // exchange sign (-1)^(l_c+l_d+L) (times -1 for the triplet)
 };
 
-// Host-side plan of one symmetry block (built from the configuration list).
+constexpr int kMaxL = 64;    // l1, l2 < 64 (channel lookup table is kMaxL x kMaxL)
+constexpr int kMaxCh = 256;  // channels per symmetry block
+
+// Host-side plan of one symmetry block: its channels (in configuration
+// order) and the angular coupling of every (row channel, column channel).
 struct BlockPlan {
     int64_t n_config = 0, L = 0, spin = 0, full = 1;
     int n_ch = 0;
-    std::vector<int> ch_l1, ch_l2;          // channel angular momenta
-    std::vector<int> row_n1, row_n2, row_ch;  // per row
-    // per channel c and n1 in [0, N+1]: first config row, n2 range (hi < lo = empty)
-    std::vector<int> seg_base, seg_lo, seg_hi;  // [n_ch][N+2]
-    std::vector<PairInfo> pairs;                // [n_ch][n_ch]
-    std::vector<int8_t> pair_k;                 // [n_ch][n_ch][2][K1]
-    std::vector<double> pair_a;                 // [n_ch][n_ch][2][K1]
-    std::vector<float> pair_af;                 // [n_ch][n_ch][2][K1][2] (hi, lo) for the mixed path
-    // tiles: distinct (n_a, n_b) with their rows
-    std::vector<int> tile_a, tile_b, tile_ptr, tile_rows;
-    bool count_mismatch = false;  // a channel pair where count_nnz and construct differ
+    std::vector<int> ch_l1, ch_l2, ch_start;  // channel angular momenta and first row
+    std::vector<PairInfo> pairs;              // [n_ch][n_ch]
+    std::vector<int8_t> pair_k;               // [n_ch][n_ch][2][K1]
+    std::vector<double> pair_a;               // [n_ch][n_ch][2][K1]
+    std::vector<float> pair_af;               // [n_ch][n_ch][2][K1][2] (hi, lo) for the mixed path
 };
 
-// Device copy of a block plan.
+// Device side of the counted block.  The configuration list itself is the
+// row table; segment tables give, per (channel c, n1), the first row and the
+// n2 range, from which the rows of a tile (n_a, n_b) follow directly.
 struct DevBlock {
-    int4 *rows = nullptr;  // (n1, n2, ch, 0) per row, 1-based n
-    int *seg = nullptr;    // base | lo | hi, each [n_ch][N+2]
+    bs2e_config *cfg = nullptr, *cfg_new = nullptr;  // uploaded configurations (current, incoming)
+    int64_t cfg_cap = 0, cfg_new_cap = 0;
+    int4 *marks = nullptr;        // channel starts found on the device (row, l1, l2, -)
+    int *lmap = nullptr;          // [kMaxL][kMaxL] -> channel index or -1
+    int *chl = nullptr;           // [n_ch] l1 << 8 | l2
+    int *seg = nullptr;           // base | lo | hi, each [n_ch][N+2]
+    int64_t seg_cap = 0;
     PairInfo *pairs = nullptr;
     int8_t *pair_k = nullptr;
     double *pair_a = nullptr;
     float *pair_af = nullptr;
-    int *tile_ab = nullptr;  // [n_tiles][2]
-    int *tile_ptr = nullptr;
-    int *tile_rows = nullptr;
-    int64_t *cntH = nullptr, *cntS = nullptr;  // per-row counts, then exclusive offsets
+    int64_t pair_cap = 0;
+    int64_t *cntH = nullptr, *cntS = nullptr;  // per-row counts
+    int64_t cnt_cap = 0;
     int64_t *scan_tmp = nullptr;
-    int64_t n_tiles = 0;
+    int64_t scan_cap = 0;
+    unsigned long long *stats = nullptr;  // [0] error bits, [1..2] count_nnz H,S, [3..4] construct H,S, [5] marks
     int64_t nnzH = -1, nnzS = -1;
-    // identity of the counted block: its parameters and a copy of its configurations
+    // identity of the counted block
     bool valid = false;
-    int64_t L = -1, spin = -1, full = -1;
-    std::vector<bs2e_config> cfg;
+    int64_t L = -1, spin = -1, full = -1, n = -1;
 };
 
 struct Radial {
@@ -93,7 +99,8 @@ struct bs2e_handle {
     std::vector<double> knots, glx, glw;
     // device radial data
     double *d_knots = nullptr, *d_glx = nullptr, *d_glw = nullptr;
-    double *d_tab_r = nullptr, *d_tab_B = nullptr, *d_tab_ri = nullptr, *d_tab_Bi = nullptr;
+    double *d_tab_r = nullptr, *d_tab_B = nullptr, *d_tab_D2 = nullptr, *d_tab_ri = nullptr,
+           *d_tab_Bi = nullptr;
     double *d_mom = nullptr, *d_dint = nullptr, *d_tot = nullptr;
     double *d_R = nullptr;      // FP64 store
     float2 *d_Rf = nullptr;     // mixed store: scaled (hi, lo) pairs, same tile layout
@@ -103,9 +110,12 @@ struct bs2e_handle {
     std::vector<char> rk_done;  // per k
     // one-body, banded complex: Hb[l][x][W], Sb[x][W]
     double2 *d_Hb = nullptr, *d_Sb = nullptr;
+    float4 *d_Hbf = nullptr, *d_Sbf = nullptr;  // same bands as FP32 pairs (mixed path)
+    int *d_flag = nullptr;                      // band values outside the FP32-pair range
     int64_t n_l = 0;
     bool have_one_body = false;
     bool s_real = true;
+    bool ff_one_body = false;  // mixed path may use the FP32-pair bands
     // block cache
     bs2e::BlockPlan plan;
     bs2e::DevBlock blk;
@@ -118,9 +128,8 @@ double ang_k_LS(int k, int la, int lb, int lc, int ld, int L);
 double three_j(int ja, int jb, int jc, int ma, int mb, int mc);
 double six_j(int ja, int jb, int jc, int jd, int je, int jf);
 void gauss_legendre(int q, double *x, double *w);
-// Builds the block plan; returns BS2E_OK or an error code with message.
-bs2e_status build_plan(const bs2e_config *cf, int64_t n_config, int64_t L, int64_t spin,
-                       int64_t full, const Radial &g, BlockPlan &plan, std::string &err);
+// Angular tables of a block from its ordered channel list.
+void plan_channels(BlockPlan &plan, int K1);
 
 // Kernel launchers (bs2e_radial.cu)
 void launch_tabulate(bs2e_handle *h);
@@ -130,7 +139,11 @@ void launch_rk_fill(bs2e_handle *h, int k_first, int k_count);
 void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *d_vals);
 void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, double cap_r0,
                      double eta_re, double eta_im);
+void launch_band_split(bs2e_handle *h);
 // Kernel launchers (bs2e_assembly.cu)
+void launch_cfg_equal(bs2e_handle *h, int64_t n);
+void launch_chan_marks(bs2e_handle *h, int64_t n);
+void launch_plan_seg(bs2e_handle *h, int64_t n);
 void launch_block_count(bs2e_handle *h);
 void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr);
 void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_Sptr,

@@ -73,7 +73,8 @@ __device__ __forceinline__ double powi(double x, int n) {
 // ---------------------------------------------------------------------------
 __global__ void k_tabulate(const double *__restrict__ knots, const double *__restrict__ glx,
                            int k, int q, double *__restrict__ tab_r, double *__restrict__ tab_B,
-                           double *__restrict__ tab_ri, double *__restrict__ tab_Bi) {
+                           double *__restrict__ tab_D2, double *__restrict__ tab_ri,
+                           double *__restrict__ tab_Bi) {
     const int iv = blockIdx.x;
     const int iv1 = iv + 1;
     const double lo = knots[k - 1 + iv], hi = knots[k + iv];
@@ -84,6 +85,7 @@ __global__ void k_tabulate(const double *__restrict__ knots, const double *__res
         double r = __dadd_rn(__dmul_rn(sc, glx[P]), tr);
         if (s == 0) tab_r[(size_t)iv * q + P] = r;
         tab_B[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 0, iv1, iv1 + s);
+        tab_D2[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 2, iv1, iv1 + s);
     }
     for (int e = threadIdx.x; e < q * q * k; e += blockDim.x) {
         int s = e % k, PQ = e / k, Q = PQ % q, P = PQ / q;
@@ -210,11 +212,49 @@ __global__ void k_totals(const double *__restrict__ mom, int k, int K1, int N, i
 //   iv1 == iv2 : D(iv; ac, bd) + D(iv; bd, ac)
 // which is compute_R_K_map (sparse_array_tools.f90:472-488).  Pairs whose
 // interval ranges do not overlap factor into one product of pair totals.
+//
+// MIXED stores each (tile, k) slice as FP32 pairs (hi, lo) of R 2^(kRkBias-e)
+// with e = ilogb(max of the slice), and e in Rexp[tile][k]: hi + lo carries
+// ~48 bits, and a slice may span up to ~2^180 before its smallest values lose
+// precision (2^108 at the N=200, k=0..10 grid).
 // ---------------------------------------------------------------------------
-__global__ void k_rk_fill(const double *__restrict__ mom, const double *__restrict__ dint,
+__device__ __forceinline__ double rk_element(const double *__restrict__ mom,
+                                            const double *__restrict__ dint,
+                                            const double *__restrict__ tot, int k, int K1, int N,
+                                            int n_iv, int a, int b, int kk, int dc, int dd) {
+    const int W = 2 * k - 1, k2 = k * k;
+    int c = a + dc - (k - 1), d = b + dd - (k - 1);
+    if (c < 0 || c >= N || d < 0 || d >= N) return 0.0;
+    int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
+    int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
+    const double *mt = tot + (size_t)kk * N * W;
+    const double *Mt = tot + ((size_t)K1 + kk) * N * W;
+    if (hip < loq) return mt[a * W + dc] * Mt[b * W + dd];
+    if (lop > hiq) return Mt[a * W + dc] * mt[b * W + dd];
+    double v = 0.0;
+    for (int iv1 = lop; iv1 <= hip; ++iv1) {
+        int pa = (a + 1 - iv1) * k + (c + 1 - iv1);
+        const double *m1 = mom + ((size_t)iv1 * K1 + kk) * 2 * k2;
+        for (int iv2 = loq; iv2 <= hiq; ++iv2) {
+            int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
+            const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
+            if (iv1 < iv2) {
+                v = fma(m1[pa], m2[k2 + pb], v);
+            } else if (iv1 > iv2) {
+                v = fma(m1[k2 + pa], m2[pb], v);
+            } else {
+                const double *D = dint + ((size_t)iv1 * K1 + kk) * (size_t)k2 * k2;
+                v += D[(size_t)pa * k2 + pb] + D[(size_t)pb * k2 + pa];
+            }
+        }
+    }
+    return v;
+}
+
+__global__ void k_rk_store(const double *__restrict__ mom, const double *__restrict__ dint,
                           const double *__restrict__ tot, int k, int K1, int N, int n_iv,
                           int64_t tile, int k_first, int k_count, double *__restrict__ R) {
-    const int W = 2 * k - 1, W2 = W * W, k2 = k * k;
+    const int W = 2 * k - 1, W2 = W * W;
     const int a = blockIdx.x / N, b = blockIdx.x - a * N;
     double *dst = R + (size_t)blockIdx.x * tile;
     const int nel = K1 * W2;
@@ -226,43 +266,57 @@ __global__ void k_rk_fill(const double *__restrict__ mom, const double *__restri
         int kk = e / W2, rem = e - kk * W2;
         if (kk < k_first || kk >= k_first + k_count) continue;
         int dc = rem / W, dd = rem - dc * W;
-        int c = a + dc - (k - 1), d = b + dd - (k - 1);
-        double v = 0.0;
-        if (c >= 0 && c < N && d >= 0 && d < N) {
-            int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-            int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
-            const double *mt = tot + (size_t)kk * N * W;
-            const double *Mt = tot + ((size_t)K1 + kk) * N * W;
-            if (hip < loq) {
-                v = mt[a * W + dc] * Mt[b * W + dd];
-            } else if (lop > hiq) {
-                v = Mt[a * W + dc] * mt[b * W + dd];
-            } else {
-                for (int iv1 = lop; iv1 <= hip; ++iv1) {
-                    int pa = (a + 1 - iv1) * k + (c + 1 - iv1);
-                    const double *m1 = mom + ((size_t)iv1 * K1 + kk) * 2 * k2;
-                    for (int iv2 = loq; iv2 <= hiq; ++iv2) {
-                        int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
-                        const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
-                        if (iv1 < iv2) {
-                            v = fma(m1[pa], m2[k2 + pb], v);
-                        } else if (iv1 > iv2) {
-                            v = fma(m1[k2 + pa], m2[pb], v);
-                        } else {
-                            const double *D = dint + ((size_t)iv1 * K1 + kk) * (size_t)k2 * k2;
-                            v += D[(size_t)pa * k2 + pb] + D[(size_t)pb * k2 + pa];
-                        }
-                    }
-                }
-            }
-        }
-        dst[e] = v;
+        dst[e] = rk_element(mom, dint, tot, k, K1, N, n_iv, a, b, kk, dc, dd);
     }
 }
 
-__global__ void k_rk_gather(const double *__restrict__ R, int k, int K1, int N, int64_t tile,
-                            int64_t n, const int64_t *__restrict__ keys,
-                            double *__restrict__ vals) {
+__global__ void k_rk_store_mixed(const double *__restrict__ mom, const double *__restrict__ dint,
+                                const double *__restrict__ tot, int k, int K1, int N, int n_iv,
+                                int64_t tile, int k_first, int k_count, float2 *__restrict__ Rf,
+                                int *__restrict__ Rexp) {
+    extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile
+    __shared__ int sexp[kMaxK1];
+    const int W = 2 * k - 1, W2 = W * W;
+    const int a = blockIdx.x / N, b = blockIdx.x - a * N;
+    const int nel = K1 * W2;
+    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
+        int kk = e / W2, rem = e - kk * W2;
+        if (kk < k_first || kk >= k_first + k_count) continue;
+        int dc = rem / W, dd = rem - dc * W;
+        sv[e] = rk_element(mom, dint, tot, k, K1, N, n_iv, a, b, kk, dc, dd);
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int kk = k_first + warp; kk < k_first + k_count; kk += nwarp) {
+        double m = 0.0;
+        for (int i = lane; i < W2; i += 32) m = fmax(m, sv[kk * W2 + i]);
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        int ex = (m > 0.0) ? ilogb(m) : 0;
+        if (lane == 0) {
+            sexp[kk] = ex;
+            Rexp[(size_t)blockIdx.x * K1 + kk] = ex;
+        }
+    }
+    __syncthreads();
+    float2 *dst = Rf + (size_t)blockIdx.x * tile;
+    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+        if (e >= nel) {
+            dst[e] = make_float2(0.f, 0.f);
+            continue;
+        }
+        int kk = e / W2;
+        if (kk < k_first || kk >= k_first + k_count) continue;
+        double scale = __longlong_as_double((long long)(1023 + kRkBias - sexp[kk]) << 52);
+        double x = sv[e] * scale;
+        float hi = __double2float_rn(x);
+        float lo = __double2float_rn(x - (double)hi);
+        dst[e] = make_float2(hi, lo);
+    }
+}
+
+__global__ void k_rk_gather(const double *__restrict__ R, const float2 *__restrict__ Rf,
+                            const int *__restrict__ Rexp, int k, int K1, int N, int64_t tile,
+                            int64_t n, const int64_t *__restrict__ keys, double *__restrict__ vals) {
     const int W = 2 * k - 1;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * K1;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -274,7 +328,16 @@ __global__ void k_rk_gather(const double *__restrict__ R, int k, int K1, int N, 
         if (a >= 0 && a < N && b >= 0 && b < N && c >= 0 && c < N && d >= 0 && d < N &&
             c - a < k && a - c < k && d - b < k && b - d < k) {
             int dc = (int)(c - a) + k - 1, dd = (int)(d - b) + k - 1;
-            v = R[(size_t)(a * N + b) * tile + ((size_t)kk * W + dc) * W + dd];
+            size_t t = (size_t)(a * N + b);
+            size_t o = t * tile + ((size_t)kk * W + dc) * W + dd;
+            if (R) {
+                v = R[o];
+            } else {
+                float2 x = Rf[o];
+                int ex = Rexp[t * K1 + kk];
+                double scale = __longlong_as_double((long long)(1023 - kRkBias + ex) << 52);
+                v = ((double)x.x + (double)x.y) * scale;
+            }
         }
         vals[e] = v;
     }
@@ -282,53 +345,71 @@ __global__ void k_rk_gather(const double *__restrict__ R, int k, int K1, int N, 
 
 // ---------------------------------------------------------------------------
 // One-body matrices (setup_S, setup_H_one_particle: mat_els.f90:47-118,
-// compute_H / compute_S :294-346) in banded form.  One thread per band entry
-// (i, j), |i-j| < k; the GL nodes of each interval are mapped as gau_leg does.
+// compute_H / compute_S :294-346) in banded form from the tabulated spline
+// values and second derivatives at the interval GL points (the points gau_leg
+// gives, quad_tools.f90:29-52).  One thread per (l, i, j) band entry, |i-j|<k:
+//   H_l(i,j) = sum w (-1/2 B_i B_j'' + (l(l+1)/(2r^2) - Z/r + CAP(r)) B_i B_j)
+// with CAP(r) = -i eta (r-r0)^order for r >= r0 (CAP_tools.f90:23-33).
 // ---------------------------------------------------------------------------
-__global__ void k_one_body(const double *__restrict__ knots, const double *__restrict__ glx,
-                           const double *__restrict__ glw, int k, int q, int N, int n_iv, int Z,
-                           int n_l, int cap_order, double cap_r0, double eta_re, double eta_im,
-                           double2 *__restrict__ Sb, double2 *__restrict__ Hb) {
+__global__ void k_one_body(const double *__restrict__ knots, const double *__restrict__ glw,
+                           const double *__restrict__ tab_r, const double *__restrict__ tab_B,
+                           const double *__restrict__ tab_D2, int k, int q, int N, int n_iv,
+                           int Z, int n_l, int cap_order, double cap_r0, double eta_re,
+                           double eta_im, double2 *__restrict__ Sb, double2 *__restrict__ Hb) {
     const int W = 2 * k - 1;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= N * W) return;
-    int i = e / W, dx = e - i * W;  // 0-based basis index i, column j = i + dx - (k-1)
-    int j = i + dx - (k - 1);
+    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= (int64_t)n_l * N * W) return;
+    const int l = (int)(e / ((int64_t)N * W));
+    const int r = (int)(e - (int64_t)l * N * W);
+    const int i = r / W, dx = r - i * W;  // 0-based basis index i, column j = i + dx - (k-1)
+    const int j = i + dx - (k - 1);
     if (j < 0 || j >= N) {
-        Sb[e] = make_double2(0.0, 0.0);
-        for (int l = 0; l < n_l; ++l) Hb[(size_t)l * N * W + e] = make_double2(0.0, 0.0);
+        Hb[e] = make_double2(0.0, 0.0);
+        if (l == 0) Sb[r] = make_double2(0.0, 0.0);
         return;
     }
-    int ib = i + 1, jb = j + 1;  // 1-based basis indices; full spline index +1
-    double s = 0.0;
-    double hre[32], him[32];
-    for (int l = 0; l < n_l; ++l) hre[l] = him[l] = 0.0;
-    int lo = max(max(i, j) - k + 2, 0), hi = min(min(i, j) + 1, n_iv - 1);
+    double s = 0.0, hre = 0.0, him = 0.0;
+    const int lo = max(max(i, j) - k + 2, 0), hi = min(min(i, j) + 1, n_iv - 1);
     for (int iv = lo; iv <= hi; ++iv) {
-        double a = knots[k - 1 + iv], b = knots[k + iv];
+        const double a = knots[k - 1 + iv], b = knots[k + iv];
+        const int si = i + 1 - iv, sj = j + 1 - iv;
         for (int P = 0; P < q; ++P) {
-            double x = 0.5 * (b - a) * glx[P] + 0.5 * (b + a);
-            double w = 0.5 * (b - a) * glw[P];
-            double Bi = bval(knots, k, x, 0, iv + 1, ib + 1);
-            double Bj = bval(knots, k, x, 0, iv + 1, jb + 1);
-            double DBj = bval(knots, k, x, 2, iv + 1, jb + 1);
+            const size_t o = ((size_t)iv * q + P) * k;
+            const double x = tab_r[(size_t)iv * q + P];
+            const double w = 0.5 * (b - a) * glw[P];
+            const double Bi = tab_B[o + si], Bj = tab_B[o + sj], DBj = tab_D2[o + sj];
             s = s + w * Bi * Bj;
             double cre = 0.0, cim = 0.0;
             if (x >= cap_r0) {
                 double pw = powi(x - cap_r0, cap_order);
-                // (0,-1) * eta * pw
-                cre = eta_im * pw;
+                cre = eta_im * pw;  // (0,-1) * eta * pw
                 cim = -eta_re * pw;
             }
-            for (int l = 0; l < n_l; ++l) {
-                double V = 0.5 * (double)l * (double)(l + 1) / (x * x) - (double)Z / x;
-                hre[l] = hre[l] + w * (-0.5 * Bi * DBj + (V + cre) * Bi * Bj);
-                him[l] = him[l] + w * (cim * Bi * Bj);
-            }
+            const double V = 0.5 * (double)l * (double)(l + 1) / (x * x) - (double)Z / x;
+            hre = hre + w * (-0.5 * Bi * DBj + (V + cre) * Bi * Bj);
+            him = him + w * (cim * Bi * Bj);
         }
     }
-    Sb[e] = make_double2(s, 0.0);
-    for (int l = 0; l < n_l; ++l) Hb[(size_t)l * N * W + e] = make_double2(hre[l], him[l]);
+    Hb[e] = make_double2(hre, him);
+    if (l == 0) Sb[r] = make_double2(s, 0.0);
+}
+
+// Splits the complex FP64 bands into FP32 pairs (re hi, re lo, im hi, im lo)
+// for the mixed assembly; flags any non-zero magnitude outside [2^-100, 2^100]
+// so the host can keep FP64 one-body products instead.
+__global__ void k_band_split(const double2 *__restrict__ src, int64_t n, float4 *__restrict__ dst,
+                             int *__restrict__ flag) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        double2 v = src[e];
+        float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
+        float rl = __double2float_rn(v.x - (double)rh), il = __double2float_rn(v.y - (double)ih);
+        dst[e] = make_float4(rh, rl, ih, il);
+        double ar = fabs(v.x), ai = fabs(v.y);
+        const double lo = 7.888609052210118e-31, hi = 1.2676506002282294e+30;  // 2^-100, 2^100
+        if ((ar != 0.0 && (ar < lo || ar > hi)) || (ai != 0.0 && (ai < lo || ai > hi)))
+            atomicOr(flag, 1);
+    }
 }
 
 }  // namespace
@@ -343,7 +424,7 @@ static inline unsigned grid_for(int64_t n, int threads) {
 void launch_tabulate(bs2e_handle *h) {
     const Radial &g = h->g;
     k_tabulate<<<g.n_iv, 128, 0, h->stream>>>(h->d_knots, h->d_glx, g.k, g.q, h->d_tab_r,
-                                               h->d_tab_B, h->d_tab_ri, h->d_tab_Bi);
+                                               h->d_tab_B, h->d_tab_D2, h->d_tab_ri, h->d_tab_Bi);
     h->launches++;
 }
 
@@ -373,25 +454,42 @@ void launch_totals(bs2e_handle *h) {
 void launch_rk_fill(bs2e_handle *h, int k_first, int k_count) {
     const Radial &g = h->g;
     unsigned tiles = (unsigned)((int64_t)g.N * g.N);
-    k_rk_fill<<<tiles, 256, 0, h->stream>>>(h->d_mom, h->d_dint, h->d_tot, g.k, g.K1, g.N, g.n_iv,
-                                            g.tile, k_first, k_count, h->d_R);
+    if (h->precision == BS2E_PREC_MIXED) {
+        size_t smem = (size_t)g.K1 * g.W * g.W * sizeof(double);
+        cudaFuncSetAttribute(k_rk_store_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_rk_store_mixed<<<tiles, 256, smem, h->stream>>>(h->d_mom, h->d_dint, h->d_tot, g.k, g.K1,
+                                                         g.N, g.n_iv, g.tile, k_first, k_count,
+                                                         h->d_Rf, h->d_Rexp);
+    } else {
+        k_rk_store<<<tiles, 256, 0, h->stream>>>(h->d_mom, h->d_dint, h->d_tot, g.k, g.K1, g.N,
+                                                g.n_iv, g.tile, k_first, k_count, h->d_R);
+    }
     h->launches++;
 }
 
 void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *d_vals) {
     const Radial &g = h->g;
-    k_rk_gather<<<grid_for(n * g.K1, 256), 256, 0, h->stream>>>(h->d_R, g.k, g.K1, g.N, g.tile, n,
-                                                                d_keys, d_vals);
+    k_rk_gather<<<grid_for(n * g.K1, 256), 256, 0, h->stream>>>(
+        h->d_R, h->d_Rf, h->d_Rexp, g.k, g.K1, g.N, g.tile, n, d_keys, d_vals);
     h->launches++;
+}
+
+void launch_band_split(bs2e_handle *h) {
+    const Radial &g = h->g;
+    int64_t nh = h->n_l * g.N * g.W, ns = (int64_t)g.N * g.W;
+    cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->stream);
+    k_band_split<<<grid_for(nh, 256), 256, 0, h->stream>>>(h->d_Hb, nh, h->d_Hbf, h->d_flag);
+    k_band_split<<<grid_for(ns, 256), 256, 0, h->stream>>>(h->d_Sb, ns, h->d_Sbf, h->d_flag);
+    h->launches += 2;
 }
 
 void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, double cap_r0,
                      double eta_re, double eta_im) {
     const Radial &g = h->g;
-    int n = g.N * g.W;
-    k_one_body<<<(n + 127) / 128, 128, 0, h->stream>>>(
-        h->d_knots, h->d_glx, h->d_glw, g.k, g.q, g.N, g.n_iv, (int)Z, (int)n_l, (int)cap_order,
-        cap_r0, eta_re, eta_im, h->d_Sb, h->d_Hb);
+    int64_t n = n_l * g.N * g.W;
+    k_one_body<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(
+        h->d_knots, h->d_glw, h->d_tab_r, h->d_tab_B, h->d_tab_D2, g.k, g.q, g.N, g.n_iv, (int)Z,
+        (int)n_l, (int)cap_order, cap_r0, eta_re, eta_im, h->d_Sb, h->d_Hb);
     h->launches++;
 }
 

@@ -20,7 +20,10 @@ cpu_baseline: the CPU oracle (C restatement of the reference, OpenMP) on a
         reference's OpenMP-over-symmetries decomposition).
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--precision fp64|mixed]
+                [--precision fp64|mixed] [--no-e2e] [--no-cpu-baseline]
+python bench.py --profile-block B   one radial pass and one count + fill of block B
+                                    (0 = L=0 singlet, 117,620 rows): the small case
+                                    for ncu captures of the fill kernel
 """
 import argparse
 import json
@@ -262,6 +265,9 @@ def run_ours(args, rank, world):
     barrier()
     t_radial = r0.elapsed_time(r1) / 1e3 / args.steps
 
+    if args.no_e2e:
+        return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, None,
+                       launches, fill_bytes, fill_s, clk, h, rank)
     # e2e through the C ABI with pinned host buffers
     del out_dev
     torch.cuda.empty_cache()
@@ -294,8 +300,16 @@ def run_ours(args, rank, world):
         step_e2e()
     barrier()
     t_e2e = _max_over_ranks((time.perf_counter() - te0) / e2e_steps, world)
-    e2e_value = world * elems / t_e2e
+    e2e = {"value": world * elems / t_e2e, "unit": "R^k elements/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "s_per_step": t_e2e}
+    return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
+                   fill_bytes, fill_s, clk, h, rank)
 
+
+def _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
+            fill_bytes, fill_s, clk, h, rank):
+    w = WORKLOAD
+    value = world * elems * args.steps / t_dev
     peak, peak_src = _peaks()
     achieved = fill_bytes * args.steps / fill_s / 1e9 if fill_s > 0 else None
     res = {
@@ -313,8 +327,7 @@ def run_ours(args, rank, world):
         "assembly_s": (t_dev / args.steps) - t_radial,
         "radial_s": t_radial,
         "rk_stage_elements_per_s": elems / t_radial,
-        "e2e": {"value": e2e_value, "unit": "R^k elements/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "s_per_step": t_e2e},
+        "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "k_fill", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
@@ -328,6 +341,38 @@ def run_ours(args, rank, world):
         res["cpu_baseline"] = {k: v for k, v in cpu_baseline(pkg, w).items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
     return res
+
+
+def profile_block(args):
+    """Small case for ncu: one radial pass, then count + fill of one block into
+    device buffers (block 0 writes ~2.9 GB of CSR, above L2, one k_fill launch)."""
+    import torch
+    pkg = _pkg()
+    w = WORKLOAD
+    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    L, par, spin, cf = workload_blocks(pkg, w)[args.profile_block]
+    with pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec) as h:
+        h.slater()
+        h.rk()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+        ch, cs = h.block_count(cf, L, w["full"], spin)
+        n = cf.size
+        dev = torch.device("cuda", 0)
+        Hd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
+                  indices=torch.empty(ch, dtype=torch.int64, device=dev),
+                  data=torch.empty(ch, dtype=torch.complex128, device=dev))
+        Sd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
+                  indices=torch.empty(cs, dtype=torch.int64, device=dev),
+                  data=torch.empty(cs, dtype=torch.complex128, device=dev))
+        torch.cuda.synchronize()
+        h.block_fill_into(cf, L, w["full"], spin, {x: v.data_ptr() for x, v in Hd.items()},
+                          {x: v.data_ptr() for x, v in Sd.items()}, on_device=True)
+        h.synchronize()
+        print(json.dumps({"profile_block": args.profile_block, "L": L, "spin": spin,
+                          "rows": int(n), "nnz_H": ch, "nnz_S": cs,
+                          "output_bytes": 24 * (ch + cs)}))
 
 
 def _max_over_ranks(x, world):
@@ -374,7 +419,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-block", type=int, default=None)
     args = ap.parse_args()
+    if args.profile_block is not None:
+        profile_block(args)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":

@@ -162,3 +162,46 @@ def test_gpu_hydrogenic_known_answer(bs2e, oracle):
     F0 = np.sum(c1[keys[:, 0]] * c1[keys[:, 1]] * c1[keys[:, 2]] * c1[keys[:, 3]] * vals)
     assert abs(e[0] + Z * Z / 2) < 1e-11
     assert abs(F0 - 5 * Z / 8) < 1e-11 * (5 * Z / 8)
+
+
+# ---------------------------------------------------------------------------
+# Mixed path: R^k stored as scaled FP32 pairs, multipole sums in FP32-pair
+# arithmetic.  Target <= 1e-9 relative (term-magnitude scale); the pairs carry
+# ~44 bits, so the bar checked here is 1e-11.
+# ---------------------------------------------------------------------------
+MIXED_RTOL = 1e-11
+
+
+@pytest.mark.parametrize("case", ["cfg1", "small2"])
+def test_mixed_rk_store_matches_oracle(bs2e, oracle, case):
+    c = CASES[case]
+    R = oracle_reference(case)["R"]
+    k, N, W = c["k"], c["n_b"], 2 * c["k"] - 1
+    a, b, dc, dd = np.meshgrid(np.arange(N), np.arange(N), np.arange(W), np.arange(W),
+                               indexing="ij")
+    cc, d = a + dc - (k - 1), b + dd - (k - 1)
+    ok = (cc >= 0) & (cc < N) & (d >= 0) & (d < N)
+    keys = np.stack([a[ok] + 1, b[ok] + 1, cc[ok] + 1, d[ok] + 1], axis=1)
+    with _handle(bs2e, case, precision=bs2e.PREC_MIXED) as h:
+        h.rk()
+        got = h.rk_get(keys)
+    np.testing.assert_allclose(got, oracle.rk_lookup(R, k, keys), rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("case", ["cfg1", "small2", "cut"])
+def test_mixed_blocks_match_oracle(bs2e, oracle, case):
+    c = CASES[case]
+    ref = oracle_reference(case)
+    worst = 0.0
+    with _handle(bs2e, case, precision=bs2e.PREC_MIXED) as h:
+        h.rk()
+        h.set_one_body(ref["H1p"], ref["S"])
+        for (L, M, par, spin, cf) in blocks(bs2e, case):
+            Hg, Sg = h.block(cf, L, True, spin)
+            Hr, Sr = oracle.construct_block(cf, L, c["k"], c["n_b"], c["max_k"], ref["R"],
+                                            ref["H1p"], ref["S"], True, spin)
+            assert_csr_close(Hg, Hr, MIXED_RTOL)
+            assert_csr_close(Sg, Sr, RTOL, with_scale=False)
+            rel = np.abs(Hg["data"] - Hr["data"]) / np.maximum(Hr["scale"], 1e-300)
+            worst = max(worst, float(rel.max()) if rel.size else 0.0)
+    print("mixed %s: max error / term scale = %.3e" % (case, worst))
