@@ -40,6 +40,7 @@ EXPORTS = [
     "bs2e_set_one_body", "bs2e_one_body", "bs2e_block_count", "bs2e_block_fill",
     "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_configs", "bs2e_ang_k_LS",
     "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
+    "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
 ]
 
 
@@ -91,6 +92,12 @@ def lib():
         "bs2e_stream": (st, [p, p]),
         "bs2e_launch_count": (st, [p, p]),
         "bs2e_synchronize": (st, [p]),
+        "bs2e_radial_dipole": (st, [p, i64, p, p, p]),
+        "bs2e_set_radial_dipole": (st, [p, i64, p, p, p]),
+        "bs2e_dip_block_count": (st, [p, p, i64, i64, i64, i64, p, i64, i64, i64, i64, i64, i64,
+                                      p]),
+        "bs2e_dip_block_fill": (st, [p, p, i64, i64, i64, i64, p, i64, i64, i64, i64, i64, i64,
+                                     p, p, p, i64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -270,6 +277,38 @@ class Bs2e:
             args += [_ptr(S[x]) for x in ("index_ptr", "indices", "data")]
         _check(self._h, lib().bs2e_block_fill_ex(self._h, _ptr(cf), cf.size, int(L), int(spin),
                                                  int(bool(full)), *args, int(bool(on_device))))
+
+    # -- dipoles ---------------------------------------------------------------
+    def radial_dipole(self, gauge=0, copy_out=True):
+        """setup_radial_dip on the device; gauge 0 = length (returns r_mat),
+        1 = velocity (returns dr_mat, r_inv_mat)."""
+        mk = lambda: np.zeros((self.n_b, self.n_b), dtype=np.complex128, order="F")
+        a = mk() if copy_out and gauge == 0 else None
+        b = mk() if copy_out and gauge == 1 else None
+        c = mk() if copy_out and gauge == 1 else None
+        _check(self._h, lib().bs2e_radial_dipole(self._h, int(gauge), _ptr(a), _ptr(b), _ptr(c)))
+        return (a,) if gauge == 0 else (b, c)
+
+    def set_radial_dipole(self, gauge, r_mat=None, dr_mat=None, r_inv_mat=None):
+        f = lambda m: None if m is None else np.asfortranarray(m, dtype=np.complex128)
+        r_mat, dr_mat, r_inv_mat = f(r_mat), f(dr_mat), f(r_inv_mat)
+        _check(self._h, lib().bs2e_set_radial_dipole(self._h, int(gauge), _ptr(r_mat),
+                                                     _ptr(dr_mat), _ptr(r_inv_mat)))
+
+    def dip_block(self, rows, sym1, cols, sym2, q, compute=True):
+        """Dipole block between symmetries sym1 = (L1, M1, parity1) (rows) and
+        sym2 = (L2, M2, parity2) (columns); returns a dict of 1-based CSR arrays."""
+        rows, cols = as_configs(rows), as_configs(cols)
+        a = [_ptr(rows), rows.size, *[int(x) for x in sym1], _ptr(cols), cols.size,
+             *[int(x) for x in sym2], int(q), int(bool(compute))]
+        n = ctypes.c_int64()
+        _check(self._h, lib().bs2e_dip_block_count(self._h, *a, ctypes.byref(n)))
+        D = dict(shape=(rows.size, cols.size), nnz=n.value,
+                 index_ptr=np.zeros(rows.size + 1, np.int64), indices=np.zeros(n.value, np.int64),
+                 data=np.zeros(n.value, np.complex128))
+        _check(self._h, lib().bs2e_dip_block_fill(self._h, *a, _ptr(D["index_ptr"]),
+                                                  _ptr(D["indices"]), _ptr(D["data"]), 0))
+        return D
 
     # -- plumbing ------------------------------------------------------------
     @property

@@ -25,44 +25,10 @@
 #include <cuda_runtime.h>
 
 #include "bs2e_internal.h"
+#include "bs2e_device.cuh"
 
 namespace bs2e {
 namespace {
-
-struct Iv2 {  // up to two disjoint ascending integer intervals [s1, s1+l1) and [s2, s2+l2)
-    int s1, l1, s2, l2;
-};
-
-__device__ __forceinline__ Iv2 make_union(int a0, int a1, bool ina, int b0, int b1, bool inb) {
-    // intervals [a0,a1] (if ina, non-empty) and [b0,b1] (if inb)
-    Iv2 r{0, 0, 0, 0};
-    bool ea = ina && a1 >= a0, eb = inb && b1 >= b0;
-    if (ea && eb) {
-        if (b0 < a0) {  // order so that a comes first
-            int t0 = a0, t1 = a1;
-            a0 = b0;
-            a1 = b1;
-            b0 = t0;
-            b1 = t1;
-        }
-        if (b0 <= a1 + 1) {  // overlap or adjacent: merge
-            r.s1 = a0;
-            r.l1 = max(a1, b1) - a0 + 1;
-        } else {
-            r.s1 = a0;
-            r.l1 = a1 - a0 + 1;
-            r.s2 = b0;
-            r.l2 = b1 - b0 + 1;
-        }
-    } else if (ea) {
-        r.s1 = a0;
-        r.l1 = a1 - a0 + 1;
-    } else if (eb) {
-        r.s1 = b0;
-        r.l1 = b1 - b0 + 1;
-    }
-    return r;
-}
 
 struct BlockArgs {
     const bs2e_config *cfg;                 // the configuration list (row table)
@@ -100,23 +66,6 @@ __device__ __forceinline__ void col_sets(const BlockArgs &A, int c_r, int c_c, i
     }
     hset = make_union(x10, x11, Aok && in_a, x20, x21, Bok && in_b);
     sset = make_union(x10, x11, leq && in_a, x20, x21, leqx && in_b);
-}
-
-// Candidate n_c values of a column channel: union of A (if a_on) and B (if b_on)
-// clipped to [nlo, N]; returned as two intervals.
-__device__ __forceinline__ Iv2 nc_candidates(int n_a, int n_b, int k, int N, bool a_on, bool b_on,
-                                             int nlo) {
-    return make_union(max(n_a - k + 1, nlo), min(n_a + k - 1, N), a_on, max(n_b - k + 1, nlo),
-                      min(n_b + k - 1, N), b_on);
-}
-
-__device__ __forceinline__ int iv2_at(const Iv2 &u, int i) {
-    return i < u.l1 ? u.s1 + i : u.s2 + (i - u.l1);
-}
-
-// Overlap length of [a0,a1] and [b0,b1].
-__device__ __forceinline__ int ovl(int a0, int a1, int b0, int b1) {
-    return max(0, min(a1, b1) - max(a0, b0) + 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -463,40 +412,26 @@ __device__ __forceinline__ FF ff_neg_if(FF a, bool neg) {
     return neg ? FF{-a.s, -a.c} : a;
 }
 
-// (s + c) * 2^shift rounded to double, assembled from the bit patterns with
-// integer arithmetic only: the pair is renormalised by TwoSum, both
-// significands are aligned in a 64-bit integer and rounded to 53 bits.  A
-// subnormal leading part (never met for in-range values) takes an FP64 path.
+// (s + c) * 2^shift as a double, assembled from the bit patterns with integer
+// instructions only (no FP64 operation): after TwoSum |c| <= ulp(s)/2, so the
+// leading part is s with its exponent rebased and its significand widened,
+// and c enters as an integer multiple of the double's ulp (its bits below that
+// ulp are truncated: at most one ulp, 2^-52 relative).  A zero or subnormal
+// leading part gives 0 (below 2^-126 of the scaled range).
 __device__ __forceinline__ double ff_to_double(FF v, int shift) {
     FF n = two_sum(v.s, v.c);
-    uint32_t us = __float_as_uint(n.s), uc = __float_as_uint(n.c);
-    int es = (int)((us >> 23) & 0xffu), ec = (int)((uc >> 23) & 0xffu);
-    if (es == 0) {
-        if ((us & 0x7fffffu) == 0) return 0.0;
-        return ((double)n.s + (double)n.c) * __longlong_as_double((long long)(1023 + shift) << 52);
+    const uint32_t us = __float_as_uint(n.s), uc = __float_as_uint(n.c);
+    const uint32_t ef = us & 0x7f800000u;
+    if (ef == 0) return 0.0;
+    long long bits = ((long long)(us & 0x7fffffffu) + ((long long)(896 + shift) << 23)) << 29;
+    const uint32_t ecf = uc & 0x7f800000u;
+    if (ecf != 0) {
+        const int sh = 29 - (int)((ef - ecf) >> 23);  // <= 5
+        const uint32_t mc = (uc & 0x7fffffu) | 0x800000u;
+        const long long add = sh >= 0 ? (long long)(mc << sh) : (sh > -24 ? (long long)(mc >> -sh) : 0);
+        bits += ((us ^ uc) >> 31) ? -add : add;
     }
-    long long M = (long long)(((uint64_t)((us & 0x7fffffu) | 0x800000u)) << 39);
-    if (ec != 0) {
-        long long mc = (long long)((uc & 0x7fffffu) | 0x800000u);
-        int sh = 39 - (es - ec);
-        long long add = sh >= 0 ? (mc << sh) : (sh > -24 ? (mc >> -sh) : 0);
-        M = ((us ^ uc) >> 31) ? M - add : M + add;
-    }
-    int p = 63 - __clzll(M);  // leading bit, 61 or 62
-    int drop = p - 52;
-    uint64_t um = (uint64_t)M;
-    uint64_t mant = um >> drop;
-    uint64_t rem = um & ((1ull << drop) - 1);
-    uint64_t half = 1ull << (drop - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) mant++;
-    if (mant >> 53) {
-        mant >>= 1;
-        p++;
-    }
-    int e2 = es - 189 + shift + p;  // exponent of the leading bit
-    uint64_t bits = ((uint64_t)(us >> 31) << 63) | ((uint64_t)(e2 + 1023) << 52) |
-                    (mant & ((1ull << 52) - 1));
-    return __longlong_as_double((long long)bits);
+    return __longlong_as_double(bits | ((long long)(us >> 31) << 63));
 }
 
 // a 2^Ea + b 2^Eb as one pair with exponent max(Ea, Eb).
@@ -567,6 +502,12 @@ __global__ void __launch_bounds__(128) k_csr_fill(FillArgs F) {
         const int row = srow[rr];
         const int c_r = sch[rr];
         const int l_a = A.chl[c_r] >> 8, l_b = A.chl[c_r] & 255;  // row channel (l1, l2)
+        // FP32-pair band rows of this row: X_row[d] = X[n][n+d], |d| < k
+        const size_t ra = (size_t)(n_a - 1) * W + (k - 1), rb = (size_t)(n_b - 1) * W + (k - 1);
+        const float4 *HaA = F.Hbf ? F.Hbf + (size_t)l_a * A.N * W + ra : nullptr;  // H_la[n_a][.]
+        const float4 *HbB = F.Hbf ? F.Hbf + (size_t)l_b * A.N * W + rb : nullptr;  // H_lb[n_b][.]
+        const float4 *SA = F.Sbf ? F.Sbf + ra : nullptr;                           // S[n_a][.]
+        const float4 *SB = F.Sbf ? F.Sbf + rb : nullptr;                           // S[n_b][.]
         int64_t oH = F.Hptr[row] - 1, oS = F.Sptr[row] - 1;
         for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
             const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
@@ -671,22 +612,22 @@ __global__ void __launch_bounds__(128) k_csr_fill(FillArgs F) {
                                 }
                                 FF hi_im{0.f, 0.f};
                                 if (one) {
-                                    // H_1p_neq (mat_els.f90:697-715) with real S
-                                    const float4 *Ha = F.Hbf + (size_t)l_a * A.N * W;
-                                    const float4 *Hbb = F.Hbf + (size_t)l_b * A.N * W;
+                                    // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
+                                    // term is non-zero only under sup, the l_eq_ex term only
+                                    // under sup_x, so both lookups stay inside the band
                                     FF hr{0.f, 0.f};
-                                    if (leq) {
-                                        float4 h1 = bandf(Ha, k, n_a, r_nc), s1 = bandf(F.Sbf, k, n_b, n_d);
-                                        float4 h2 = bandf(Hbb, k, n_b, n_d), s2 = bandf(F.Sbf, k, n_a, r_nc);
+                                    if (leq && sup) {
+                                        const int dc = r_nc - n_a, dd = n_d - n_b;
+                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
                                         float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
                                         hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
                                                     ff_mul(make_float2(h2.x, h2.y), s2r));
                                         hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
                                                        ff_mul(make_float2(h2.z, h2.w), s2r));
                                     }
-                                    if (leqx) {
-                                        float4 h1 = bandf(Ha, k, n_a, n_d), s1 = bandf(F.Sbf, k, n_b, r_nc);
-                                        float4 h2 = bandf(Hbb, k, n_b, r_nc), s2 = bandf(F.Sbf, k, n_a, n_d);
+                                    if (leqx && supx) {
+                                        const int dc = n_d - n_a, dd = r_nc - n_b;
+                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
                                         float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
                                         bool ng = pi.sgn < 0.0;
                                         FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
@@ -793,12 +734,14 @@ __global__ void __launch_bounds__(128) k_csr_fill(FillArgs F) {
                             double2 s1 = make_double2(0.0, 0.0);
                             if (MIXED && F.ff_one_body) {
                                 FF t{0.f, 0.f};
-                                if (leq) {
-                                    float4 a = bandf(F.Sbf, k, n_a, r_nc), b = bandf(F.Sbf, k, n_b, n_d);
+                                const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
+                                const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
+                                if (leq && sup) {
+                                    float4 a = SA[r_nc - n_a], b = SB[n_d - n_b];
                                     t = ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y));
                                 }
-                                if (leqx) {
-                                    float4 a = bandf(F.Sbf, k, n_a, n_d), b = bandf(F.Sbf, k, n_b, r_nc);
+                                if (leqx && supx) {
+                                    float4 a = SA[n_d - n_a], b = SB[r_nc - n_b];
                                     t = ff_add(t, ff_neg_if(ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y)),
                                                             pi.sgn < 0.0));
                                 }
@@ -860,6 +803,20 @@ void launch_cfg_equal(bs2e_handle *h, int64_t n) {
     h->launches++;
 }
 
+void launch_chan_marks_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, int4 *marks, int cap,
+                          unsigned long long *stats) {
+    if (n <= 0) return;
+    k_chan_marks<<<grid_rows(n), 256, 0, h->stream>>>(cfg, n, h->g.N, marks, cap, stats);
+    h->launches++;
+}
+
+void launch_plan_seg_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, const int *lmap,
+                        int segS, int *base, int *lo, int *hi, unsigned long long *stats) {
+    if (n <= 0) return;
+    k_plan_seg<<<grid_rows(n), 256, 0, h->stream>>>(cfg, n, lmap, segS, base, lo, hi, stats);
+    h->launches++;
+}
+
 void launch_chan_marks(bs2e_handle *h, int64_t n) {
     if (n <= 0) return;
     k_chan_marks<<<grid_rows(n), 256, 0, h->stream>>>(h->blk.cfg_new, n, h->g.N, h->blk.marks,
@@ -887,7 +844,7 @@ void launch_block_count(bs2e_handle *h) {
     }
 }
 
-static void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr) {
+void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr) {
     int64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb < 1) nb = 1;
     k_scan_partials<<<(unsigned)nb, kScanThreads, 0, h->stream>>>(in, n, part);

@@ -89,7 +89,7 @@ void free_block(DevBlock &b) {
     dfree(b.cntS);
     dfree(b.scan_tmp);
     dfree(b.stats);
-    b.cfg_cap = b.cfg_new_cap = b.seg_cap = b.pair_cap = b.cnt_cap = b.scan_cap = 0;
+    b.cfg_cap = b.cfg_new_cap = b.seg_cap = b.pair_cap = b.cntH_cap = b.cntS_cap = b.scan_cap = 0;
     b.nnzH = b.nnzS = -1;
     b.valid = false;
 }
@@ -202,9 +202,8 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
     CU(cudaMemsetAsync(B.seg + nseg, 0x7f, sizeof(int) * nseg, h->stream));       // lo = big
     CU(cudaMemsetAsync(B.seg + 2 * nseg, 0x00, sizeof(int) * nseg, h->stream));   // hi = 0
     launch_plan_seg(h, n_config);
-    CU(grow(&B.cntH, B.cnt_cap, n_config));
-    int64_t cap2 = B.cnt_cap;
-    CU(grow(&B.cntS, cap2, n_config));
+    CU(grow(&B.cntH, B.cntH_cap, n_config));
+    CU(grow(&B.cntS, B.cntS_cap, n_config));
     CU(grow(&B.scan_tmp, B.scan_cap, (n_config + 4095) / 4096 + 4));
     launch_block_count(h);
     CU(cudaMemcpyAsync(st, B.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
@@ -246,6 +245,176 @@ bs2e_status finish_one_body(bs2e_handle *h) {
     CU(cudaMemcpyAsync(&flag, h->d_flag, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     TRY(sync_check(h, "one-body split"));
     h->ff_one_body = h->s_real && flag == 0;
+    return BS2E_OK;
+}
+
+// One-particle reduced dipole dip_red_1p_len / _vel (mat_els.f90:772-809) as
+// (alpha, beta): length alpha M1 with M1 = r_mat, velocity alpha M1 + beta M2
+// with M1 = dr_mat, M2 = r_inv_mat.
+void red1p(int gauge, int l, int lp, double &al, double &be) {
+    al = be = 0.0;
+    if (gauge == 0) {
+        double sg = (l & 1) ? -1.0 : 1.0;
+        al = sg * std::sqrt((double)((2 * l + 1) * (2 * lp + 1))) * three_j(l, 1, lp, 0, 0, 0);
+        return;
+    }
+    if (std::abs(l - lp) != 1) return;
+    if (l > lp) {
+        al = std::sqrt((double)l);
+        be = -(double)(lp + 1) * std::sqrt((double)l);
+    } else {
+        al = -std::sqrt((double)lp);
+        be = -(double)lp * std::sqrt((double)lp);
+    }
+}
+
+double c_red1(int a, int b) {  // C_red_mat(1, a, b)
+    double sg = (a & 1) ? -1.0 : 1.0;
+    return sg * std::sqrt((double)((2 * a + 1) * (2 * b + 1))) * three_j(a, 1, b, 0, 0, 0);
+}
+
+// Channel-pair coefficients of a dipole block (dip_mat_neq / dip_red_mat,
+// mat_els.f90:717-770; ang_dip_red :811-828).
+DipPair dip_pair(int L1, int L2, double ang3j, int gauge, int la, int lb, int lc, int ld) {
+    DipPair p{};
+    double adr = 0.0;
+    if (lb == ld) adr += std::fabs(six_j(L1, 1, L2, lc, lb, la) * c_red1(la, lc));
+    if (la == lc) adr += std::fabs(six_j(L1, 1, L2, ld, la, lb) * c_red1(lb, ld));
+    p.ok = adr > 5e-16;
+    const double sq = std::sqrt((double)((2 * L1 + 1) * (2 * L2 + 1)));
+    const double sgx = ((L2 + lc + ld) & 1) ? -1.0 : 1.0;
+    double al, be, f;
+    if (lb == ld) {  // res_1: (n_a, n_c) with S(n_b, n_d)
+        f = (((la + lb + L2 + 1) & 1) ? -1.0 : 1.0) * sq * six_j(L1, 1, L2, lc, lb, la) * ang3j;
+        red1p(gauge, la, lc, al, be);
+        p.c[0] = f * al;
+        p.c[1] = f * be;
+    }
+    if (la == lc) {  // res_2: (n_b, n_d) with S(n_a, n_c)
+        f = (((la + ld + L1 + 1) & 1) ? -1.0 : 1.0) * sq * six_j(L1, 1, L2, ld, la, lb) * ang3j;
+        red1p(gauge, lb, ld, al, be);
+        p.c[2] = f * al;
+        p.c[3] = f * be;
+    }
+    if (lb == lc) {  // exchange res_1: (n_a, n_d) with S(n_b, n_c)
+        f = sgx * (((la + lb + L2 + 1) & 1) ? -1.0 : 1.0) * sq * six_j(L1, 1, L2, ld, lb, la) * ang3j;
+        red1p(gauge, la, ld, al, be);
+        p.c[4] = f * al;
+        p.c[5] = f * be;
+    }
+    if (la == ld) {  // exchange res_2: (n_b, n_c) with S(n_a, n_d)
+        f = sgx * (((la + lc + L1 + 1) & 1) ? -1.0 : 1.0) * sq * six_j(L1, 1, L2, lc, la, lb) * ang3j;
+        red1p(gauge, lb, lc, al, be);
+        p.c[6] = f * al;
+        p.c[7] = f * be;
+    }
+    return p;
+}
+
+// Channel runs of a configuration list found on the device, in row order.
+bs2e_status dip_channels(bs2e_handle *h, const bs2e_config *d_cfg, int64_t n,
+                         std::vector<int4> &marks) {
+    CU(cudaMemsetAsync(h->d_dip_stats, 0, 8 * sizeof(unsigned long long), h->stream));
+    launch_chan_marks_on(h, d_cfg, n, h->d_dip_marks, kMaxCh + 1, h->d_dip_stats);
+    unsigned long long st[8];
+    marks.assign(kMaxCh + 1, make_int4(0, 0, 0, 0));
+    CU(cudaMemcpyAsync(st, h->d_dip_stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(marks.data(), h->d_dip_marks, sizeof(int4) * marks.size(),
+                       cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "dipole plan"));
+    if (st[0] & 1ull) return fail(h, BS2E_ERR_ARG, "a configuration has n or l out of range");
+    if (st[5] > (unsigned long long)kMaxCh)
+        return fail(h, BS2E_ERR_ARG, "more than 256 channel runs in one symmetry");
+    marks.resize((size_t)st[5]);
+    std::sort(marks.begin(), marks.end(), [](const int4 &a, const int4 &b) { return a.x < b.x; });
+    return BS2E_OK;
+}
+
+// Uploads, plans and counts one dipole block.  empty = the reference's
+// zero block (3j factor below 5e-16, parity not changing, or compute = 0).
+bs2e_status dip_prepare(bs2e_handle *h, const bs2e_config *rows, int64_t n_rows, int64_t L1,
+                        int64_t M1, int64_t pi1, const bs2e_config *cols, int64_t n_cols,
+                        int64_t L2, int64_t M2, int64_t pi2, int64_t q, int64_t compute,
+                        DipDev &D, bool &empty, int64_t &nnz) {
+    if (n_rows < 0 || n_cols < 0 || (n_rows > 0 && !rows) || (n_cols > 0 && !cols) || q < -1 ||
+        q > 1 || L1 < 0 || L2 < 0)
+        return fail(h, BS2E_ERR_ARG, "invalid dipole block arguments");
+    if (h->dip_gauge < 0) return fail(h, BS2E_ERR_STATE, "radial dipole matrices not set");
+    if (!h->have_one_body) return fail(h, BS2E_ERR_STATE, "overlap S not set (bs2e_set_one_body)");
+    const Radial &g = h->g;
+    double ang3j = (((L1 - M1) & 1) ? -1.0 : 1.0) *
+                   three_j((int)L1, 1, (int)L2, (int)-M1, (int)q, (int)M2);
+    bool parity_allowed = (pi1 != 0) != (pi2 != 0);
+    empty = std::fabs(ang3j) < 5e-16 || !parity_allowed || !compute || n_rows == 0 || n_cols == 0;
+    nnz = 0;
+    if (empty) return BS2E_OK;
+    if (!h->d_dip_stats) CU(dalloc(&h->d_dip_stats, 8));
+    if (!h->d_dip_marks) CU(dalloc(&h->d_dip_marks, kMaxCh + 1));
+    if (!h->d_dip_lmap) CU(dalloc(&h->d_dip_lmap, (size_t)2 * kMaxL * kMaxL));
+    CU(grow(&h->d_dip_rows, h->dip_rows_cap, n_rows));
+    CU(grow(&h->d_dip_cols, h->dip_cols_cap, n_cols));
+    CU(cudaMemcpyAsync(h->d_dip_rows, rows, sizeof(bs2e_config) * n_rows, cudaMemcpyHostToDevice,
+                       h->stream));
+    CU(cudaMemcpyAsync(h->d_dip_cols, cols, sizeof(bs2e_config) * n_cols, cudaMemcpyHostToDevice,
+                       h->stream));
+    std::vector<int4> rm, cm;
+    TRY(dip_channels(h, h->d_dip_rows, n_rows, rm));
+    TRY(dip_channels(h, h->d_dip_cols, n_cols, cm));
+    std::vector<int> lmap((size_t)2 * kMaxL * kMaxL, -1);
+    std::vector<int> rl1, rl2, cl1, cl2;
+    for (const int4 &m : rm) {  // rows: a channel may appear in several runs
+        int &slot = lmap[(size_t)m.y * kMaxL + m.z];
+        if (slot < 0) {
+            slot = (int)rl1.size();
+            rl1.push_back(m.y);
+            rl2.push_back(m.z);
+        }
+    }
+    for (const int4 &m : cm) {  // columns: each channel one contiguous run
+        int &slot = lmap[(size_t)kMaxL * kMaxL + (size_t)m.y * kMaxL + m.z];
+        if (slot >= 0)
+            return fail(h, BS2E_ERR_ORDER, "a column channel is not contiguous in the configuration list");
+        slot = (int)cl1.size();
+        cl1.push_back(m.y);
+        cl2.push_back(m.z);
+    }
+    const int nr = (int)rl1.size(), nc = (int)cl1.size();
+    std::vector<DipPair> pairs((size_t)nr * nc);
+    for (int r = 0; r < nr; ++r)
+        for (int c = 0; c < nc; ++c)
+            pairs[(size_t)r * nc + c] = dip_pair((int)L1, (int)L2, ang3j, h->dip_gauge, rl1[r],
+                                                 rl2[r], cl1[c], cl2[c]);
+    CU(grow(&h->d_dip_pairs, h->dip_pairs_cap, (int64_t)pairs.size()));
+    CU(cudaMemcpyAsync(h->d_dip_pairs, pairs.data(), sizeof(DipPair) * pairs.size(),
+                       cudaMemcpyHostToDevice, h->stream));
+    CU(cudaMemcpyAsync(h->d_dip_lmap, lmap.data(), sizeof(int) * lmap.size(),
+                       cudaMemcpyHostToDevice, h->stream));
+    const int S = g.N + 2;
+    const int64_t nseg = (int64_t)nc * S;
+    CU(grow(&h->d_dip_seg, h->dip_seg_cap, 3 * nseg));
+    CU(cudaMemsetAsync(h->d_dip_seg, 0xff, sizeof(int) * nseg, h->stream));
+    CU(cudaMemsetAsync(h->d_dip_seg + nseg, 0x7f, sizeof(int) * nseg, h->stream));
+    CU(cudaMemsetAsync(h->d_dip_seg + 2 * nseg, 0x00, sizeof(int) * nseg, h->stream));
+    CU(cudaMemsetAsync(h->d_dip_stats, 0, 8 * sizeof(unsigned long long), h->stream));
+    launch_plan_seg_on(h, h->d_dip_cols, n_cols, h->d_dip_lmap + kMaxL * kMaxL, S, h->d_dip_seg,
+                       h->d_dip_seg + nseg, h->d_dip_seg + 2 * nseg, h->d_dip_stats);
+    D.rows = h->d_dip_rows;
+    D.n_rows = n_rows;
+    D.lmap_r = h->d_dip_lmap;
+    D.seg = h->d_dip_seg;
+    D.nseg = nseg;
+    D.n_ch_r = nr;
+    D.n_ch_c = nc;
+    D.pairs = h->d_dip_pairs;
+    D.stats = h->d_dip_stats;
+    CU(grow(&h->d_dip_cnt, h->dip_cnt_cap, n_rows));
+    launch_dip_count(h, D, h->d_dip_cnt);
+    unsigned long long st[8];
+    CU(cudaMemcpyAsync(st, h->d_dip_stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "dipole count"));
+    if (st[0] & 2ull)
+        return fail(h, BS2E_ERR_ORDER, "column configurations are not in basis order");
+    nnz = (int64_t)st[3];
     return BS2E_OK;
 }
 
@@ -313,6 +482,7 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
     bad(dalloc(&h->d_tab_r, niv * q));
     bad(dalloc(&h->d_tab_B, niv * q * kk));
     bad(dalloc(&h->d_tab_D2, niv * q * kk));
+    bad(dalloc(&h->d_tab_D1, niv * q * kk));
     bad(dalloc(&h->d_tab_ri, niv * q * q));
     bad(dalloc(&h->d_tab_Bi, niv * q * q * kk));
     bad(dalloc(&h->d_mom, niv * K1 * 2 * kk * kk));
@@ -349,6 +519,18 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_tab_r);
         dfree(h->d_tab_B);
         dfree(h->d_tab_D2);
+        dfree(h->d_tab_D1);
+        dfree(h->d_dM1);
+        dfree(h->d_dM2);
+        dfree(h->d_dip_rows);
+        dfree(h->d_dip_cols);
+        dfree(h->d_dip_lmap);
+        dfree(h->d_dip_seg);
+        dfree(h->d_dip_pairs);
+        dfree(h->d_dip_marks);
+        dfree(h->d_dip_stats);
+        dfree(h->d_dip_cnt);
+        dfree(h->d_dip_part);
         dfree(h->d_tab_ri);
         dfree(h->d_tab_Bi);
         dfree(h->d_mom);
@@ -696,6 +878,133 @@ BS2E_API bs2e_status bs2e_block_fill(bs2e_handle *h, const bs2e_config *configs,
     }
     return bs2e_block_fill_ex(h, configs, n_config, L, 0, full, H_index_ptr, H_indices, H_data,
                               S_index_ptr, S_indices, S_data, 0);
+}
+
+BS2E_API bs2e_status bs2e_radial_dipole(bs2e_handle *h, int64_t gauge, double *r_mat,
+                                        double *dr_mat, double *r_inv_mat) {
+    if (!h || (gauge != 0 && gauge != 1)) return BS2E_ERR_ARG;
+    Guard G(h);
+    if (!h->slater_done) return fail(h, BS2E_ERR_STATE, "bs2e_slater has not run (tabulation)");
+    const Radial &g = h->g;
+    const int N = g.N, W = g.W, k = g.k;
+    dfree(h->d_dM1);
+    dfree(h->d_dM2);
+    CU(dalloc(&h->d_dM1, (size_t)N * W));
+    if (gauge == 1) CU(dalloc(&h->d_dM2, (size_t)N * W));
+    launch_radial_dip(h, (int)gauge);
+    TRY(sync_check(h, "radial dipole"));
+    h->dip_gauge = (int)gauge;
+    double *outs[2] = {gauge == 0 ? r_mat : dr_mat, gauge == 1 ? r_inv_mat : nullptr};
+    double2 *src[2] = {h->d_dM1, h->d_dM2};
+    for (int m = 0; m < 2; ++m) {
+        if (!outs[m] || !src[m]) continue;
+        std::vector<double2> b((size_t)N * W);
+        CU(cudaMemcpy(b.data(), src[m], b.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+        memset(outs[m], 0, sizeof(double) * 2 * (size_t)N * N);
+        for (int x = 0; x < N; ++x)
+            for (int d = 0; d < W; ++d) {
+                int y = x + d - (k - 1);
+                if (y < 0 || y >= N) continue;
+                size_t o = ((size_t)y * N + x) * 2;
+                outs[m][o] = b[(size_t)x * W + d].x;
+                outs[m][o + 1] = b[(size_t)x * W + d].y;
+            }
+    }
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_set_radial_dipole(bs2e_handle *h, int64_t gauge, const double *r_mat,
+                                            const double *dr_mat, const double *r_inv_mat) {
+    if (!h || (gauge != 0 && gauge != 1)) return BS2E_ERR_ARG;
+    if ((gauge == 0 && !r_mat) || (gauge == 1 && (!dr_mat || !r_inv_mat))) return BS2E_ERR_ARG;
+    Guard G(h);
+    const Radial &g = h->g;
+    const int N = g.N, W = g.W, k = g.k;
+    const double *ins[2] = {gauge == 0 ? r_mat : dr_mat, gauge == 1 ? r_inv_mat : nullptr};
+    dfree(h->d_dM1);
+    dfree(h->d_dM2);
+    double2 **dst[2] = {&h->d_dM1, &h->d_dM2};
+    for (int m = 0; m < 2; ++m) {
+        if (!ins[m]) continue;
+        std::vector<double2> b((size_t)N * W, make_double2(0.0, 0.0));
+        for (int x = 0; x < N; ++x)
+            for (int d = 0; d < W; ++d) {
+                int y = x + d - (k - 1);
+                if (y < 0 || y >= N) continue;
+                size_t o = ((size_t)y * N + x) * 2;
+                b[(size_t)x * W + d] = make_double2(ins[m][o], ins[m][o + 1]);
+            }
+        CU(dalloc(dst[m], b.size()));
+        CU(cudaMemcpy(*dst[m], b.data(), b.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    }
+    h->dip_gauge = (int)gauge;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_dip_block_count(bs2e_handle *h, const bs2e_config *rows, int64_t n_rows,
+                                          int64_t L1, int64_t M1, int64_t pi1,
+                                          const bs2e_config *cols, int64_t n_cols, int64_t L2,
+                                          int64_t M2, int64_t pi2, int64_t q, int64_t compute,
+                                          int64_t *nnz) {
+    if (!h || !nnz) return BS2E_ERR_ARG;
+    Guard G(h);
+    DipDev D;
+    bool empty;
+    return dip_prepare(h, rows, n_rows, L1, M1, pi1, cols, n_cols, L2, M2, pi2, q, compute, D,
+                       empty, *nnz);
+}
+
+BS2E_API bs2e_status bs2e_dip_block_fill(bs2e_handle *h, const bs2e_config *rows, int64_t n_rows,
+                                         int64_t L1, int64_t M1, int64_t pi1,
+                                         const bs2e_config *cols, int64_t n_cols, int64_t L2,
+                                         int64_t M2, int64_t pi2, int64_t q, int64_t compute,
+                                         int64_t *index_ptr, int64_t *indices, double *data,
+                                         int64_t out_on_device) {
+    if (!h || !index_ptr) return BS2E_ERR_ARG;
+    Guard G(h);
+    DipDev D;
+    bool empty;
+    int64_t nnz = 0;
+    TRY(dip_prepare(h, rows, n_rows, L1, M1, pi1, cols, n_cols, L2, M2, pi2, q, compute, D, empty,
+                    nnz));
+    const bool dev = out_on_device != 0;
+    if (empty) {
+        std::vector<int64_t> ones((size_t)n_rows + 1, 1);
+        if (dev)
+            CU(cudaMemcpy(index_ptr, ones.data(), sizeof(int64_t) * ones.size(),
+                          cudaMemcpyHostToDevice));
+        else
+            memcpy(index_ptr, ones.data(), sizeof(int64_t) * ones.size());
+        return BS2E_OK;
+    }
+    if (nnz > 0 && (!indices || !data)) return fail(h, BS2E_ERR_ARG, "NULL output array");
+    int64_t *dp = index_ptr, *di = indices;
+    double2 *dd = (double2 *)data;
+    if (!dev) {
+        CU(dalloc(&dp, (size_t)n_rows + 1));
+        CU(dalloc(&di, (size_t)nnz));
+        CU(dalloc(&dd, (size_t)nnz));
+    }
+    CU(grow(&h->d_dip_part, h->dip_part_cap, (n_rows + 4095) / 4096 + 4));
+    scan_one(h, h->d_dip_cnt, n_rows, h->d_dip_part, dp);
+    launch_dip_fill(h, D, dp, di, dd);
+    bs2e_status st = BS2E_OK;
+    if (!dev) {
+        cudaError_t e = cudaMemcpyAsync(index_ptr, dp, sizeof(int64_t) * (n_rows + 1),
+                                        cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess && nnz)
+            e = cudaMemcpyAsync(indices, di, sizeof(int64_t) * nnz, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess && nnz)
+            e = cudaMemcpyAsync(data, dd, sizeof(double2) * nnz, cudaMemcpyDeviceToHost, h->stream);
+        if (e != cudaSuccess) st = fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+    }
+    bs2e_status st2 = sync_check(h, "dipole fill");
+    if (!dev) {
+        cudaFree(dp);
+        cudaFree(di);
+        cudaFree(dd);
+    }
+    return st != BS2E_OK ? st : st2;
 }
 
 BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream) {

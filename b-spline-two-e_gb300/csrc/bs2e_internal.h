@@ -71,7 +71,7 @@ struct DevBlock {
     float *pair_af = nullptr;
     int64_t pair_cap = 0;
     int64_t *cntH = nullptr, *cntS = nullptr;  // per-row counts
-    int64_t cnt_cap = 0;
+    int64_t cntH_cap = 0, cntS_cap = 0;
     int64_t *scan_tmp = nullptr;
     int64_t scan_cap = 0;
     unsigned long long *stats = nullptr;  // [0] error bits, [1..2] count_nnz H,S, [3..4] construct H,S, [5] marks
@@ -79,6 +79,26 @@ struct DevBlock {
     // identity of the counted block
     bool valid = false;
     int64_t L = -1, spin = -1, full = -1, n = -1;
+};
+
+// Dipole coupling of one (row channel, column channel) pair: c[0..7] are the
+// (alpha, beta) coefficients of the four one-particle terms, with the 3j
+// factor, the 6j/sqrt factors and the exchange phase folded in.
+struct DipPair {
+    int32_t ok, pad;
+    double c[8];
+};
+
+// Device view of one dipole block being assembled.
+struct DipDev {
+    const bs2e_config *rows = nullptr;
+    int64_t n_rows = 0;
+    const int *lmap_r = nullptr;
+    int *seg = nullptr;  // column segment tables base | lo | hi
+    int64_t nseg = 0;
+    int n_ch_r = 0, n_ch_c = 0;
+    const DipPair *pairs = nullptr;
+    unsigned long long *stats = nullptr;
 };
 
 struct Radial {
@@ -99,6 +119,7 @@ struct bs2e_handle {
     std::vector<double> knots, glx, glw;
     // device radial data
     double *d_knots = nullptr, *d_glx = nullptr, *d_glw = nullptr;
+    double *d_tab_D1 = nullptr;  // first derivatives (velocity-gauge dipoles)
     double *d_tab_r = nullptr, *d_tab_B = nullptr, *d_tab_D2 = nullptr, *d_tab_ri = nullptr,
            *d_tab_Bi = nullptr;
     double *d_mom = nullptr, *d_dint = nullptr, *d_tot = nullptr;
@@ -119,6 +140,19 @@ struct bs2e_handle {
     // block cache
     bs2e::BlockPlan plan;
     bs2e::DevBlock blk;
+    // radial dipole bands (M1, M2) and dipole-block work buffers
+    double2 *d_dM1 = nullptr, *d_dM2 = nullptr;
+    int dip_gauge = -1;
+    bs2e_config *d_dip_rows = nullptr, *d_dip_cols = nullptr;
+    int64_t dip_rows_cap = 0, dip_cols_cap = 0;
+    int *d_dip_lmap = nullptr, *d_dip_seg = nullptr;
+    int64_t dip_seg_cap = 0;
+    bs2e::DipPair *d_dip_pairs = nullptr;
+    int64_t dip_pairs_cap = 0;
+    int4 *d_dip_marks = nullptr;
+    unsigned long long *d_dip_stats = nullptr;
+    int64_t *d_dip_cnt = nullptr, *d_dip_part = nullptr;
+    int64_t dip_cnt_cap = 0, dip_part_cap = 0;
 };
 
 namespace bs2e {
@@ -140,11 +174,21 @@ void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *
 void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, double cap_r0,
                      double eta_re, double eta_im);
 void launch_band_split(bs2e_handle *h);
+// Kernel launchers (bs2e_dipole.cu)
+void launch_radial_dip(bs2e_handle *h, int gauge);
+void launch_dip_count(bs2e_handle *h, const DipDev &D, int64_t *cnt);
+void launch_dip_fill(bs2e_handle *h, const DipDev &D, const int64_t *ptr, int64_t *idx,
+                     double2 *dat);
 // Kernel launchers (bs2e_assembly.cu)
 void launch_cfg_equal(bs2e_handle *h, int64_t n);
 void launch_chan_marks(bs2e_handle *h, int64_t n);
 void launch_plan_seg(bs2e_handle *h, int64_t n);
 void launch_block_count(bs2e_handle *h);
+void launch_chan_marks_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, int4 *marks, int cap,
+                          unsigned long long *stats);
+void launch_plan_seg_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, const int *lmap,
+                        int segS, int *base, int *lo, int *hi, unsigned long long *stats);
+void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr);
 void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr);
 void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_Sptr,
                        int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx, double2 *d_Sdat);

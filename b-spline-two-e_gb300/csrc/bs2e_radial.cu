@@ -73,8 +73,8 @@ __device__ __forceinline__ double powi(double x, int n) {
 // ---------------------------------------------------------------------------
 __global__ void k_tabulate(const double *__restrict__ knots, const double *__restrict__ glx,
                            int k, int q, double *__restrict__ tab_r, double *__restrict__ tab_B,
-                           double *__restrict__ tab_D2, double *__restrict__ tab_ri,
-                           double *__restrict__ tab_Bi) {
+                           double *__restrict__ tab_D2, double *__restrict__ tab_D1,
+                           double *__restrict__ tab_ri, double *__restrict__ tab_Bi) {
     const int iv = blockIdx.x;
     const int iv1 = iv + 1;
     const double lo = knots[k - 1 + iv], hi = knots[k + iv];
@@ -86,6 +86,7 @@ __global__ void k_tabulate(const double *__restrict__ knots, const double *__res
         if (s == 0) tab_r[(size_t)iv * q + P] = r;
         tab_B[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 0, iv1, iv1 + s);
         tab_D2[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 2, iv1, iv1 + s);
+        tab_D1[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 1, iv1, iv1 + s);
     }
     for (int e = threadIdx.x; e < q * q * k; e += blockDim.x) {
         int s = e % k, PQ = e / k, Q = PQ % q, P = PQ / q;
@@ -424,7 +425,8 @@ static inline unsigned grid_for(int64_t n, int threads) {
 void launch_tabulate(bs2e_handle *h) {
     const Radial &g = h->g;
     k_tabulate<<<g.n_iv, 128, 0, h->stream>>>(h->d_knots, h->d_glx, g.k, g.q, h->d_tab_r,
-                                               h->d_tab_B, h->d_tab_D2, h->d_tab_ri, h->d_tab_Bi);
+                                               h->d_tab_B, h->d_tab_D2, h->d_tab_D1, h->d_tab_ri,
+                                               h->d_tab_Bi);
     h->launches++;
 }
 

@@ -184,6 +184,38 @@ BS2E_API double bs2e_three_j(int64_t ja, int64_t jb, int64_t jc, int64_t ma, int
 BS2E_API double bs2e_six_j(int64_t ja, int64_t jb, int64_t jc, int64_t jd, int64_t je,
                            int64_t jf);
 
+/* Radial dipole matrices on the device, as setup_radial_dip
+ * (src/mat_els/mat_els.f90:120-170, 348-390): gauge 0 = length ('l', r_mat),
+ * 1 = velocity ('v', dr_mat and r_inv_mat).  Needs bs2e_slater (tabulation).
+ * Optional dense complex n_b x n_b copies out (NULL to skip). */
+BS2E_API bs2e_status bs2e_radial_dipole(bs2e_handle *h, int64_t gauge, double *r_mat,
+                                        double *dr_mat, double *r_inv_mat);
+
+/* Uses caller-computed radial dipole matrices (type(radial_dipole) of
+ * mat_els.f90:14-19): complex n_b x n_b column-major; length gauge needs r_mat,
+ * velocity gauge dr_mat and r_inv_mat (the others may be NULL). */
+BS2E_API bs2e_status bs2e_set_radial_dipole(bs2e_handle *h, int64_t gauge, const double *r_mat,
+                                            const double *dr_mat, const double *r_inv_mat);
+
+/* Dipole block between row symmetry (L1, M1, parity pi1) and column symmetry
+ * (L2, M2, pi2) for polarisation q in {-1, 0, 1}: construct_dip_block_tensor
+ * with init_dip_block (src/mat_els/dipole.f90:8-47, 87-146).  compute = 0
+ * gives the empty block the reference stores for skipped pairs
+ * (main_basis_setup.f90:133-137).  Uses the overlap S set by
+ * bs2e_set_one_body / bs2e_one_body.  The fill writes a 1-based CSR of shape
+ * n_rows x n_cols; an empty block gets index_ptr = 1 everywhere. */
+BS2E_API bs2e_status bs2e_dip_block_count(bs2e_handle *h, const bs2e_config *rows, int64_t n_rows,
+                                          int64_t L1, int64_t M1, int64_t pi1,
+                                          const bs2e_config *cols, int64_t n_cols, int64_t L2,
+                                          int64_t M2, int64_t pi2, int64_t q, int64_t compute,
+                                          int64_t *nnz);
+BS2E_API bs2e_status bs2e_dip_block_fill(bs2e_handle *h, const bs2e_config *rows, int64_t n_rows,
+                                         int64_t L1, int64_t M1, int64_t pi1,
+                                         const bs2e_config *cols, int64_t n_cols, int64_t L2,
+                                         int64_t M2, int64_t pi2, int64_t q, int64_t compute,
+                                         int64_t *index_ptr, int64_t *indices, double *data,
+                                         int64_t out_on_device);
+
 /* The CUDA stream all work of the handle runs on (cudaStream_t as void*), the
  * number of kernels the handle has launched so far, and a full synchronize. */
 BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream);

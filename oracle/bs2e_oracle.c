@@ -724,3 +724,130 @@ void or_setup_H1p(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
             }
         }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Dipole blocks (mat_els.f90:120-170, 348-390, 717-829; dipole.f90:8-146)    */
+/* ------------------------------------------------------------------------ */
+
+void or_setup_radial_dip(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
+                         int64_t gauge, double *r_mat, double *dr_mat, double *r_inv_mat) {
+    int64_t n = n_knots - k, nb = n - 2, n_iv = n_knots - 2 * k + 1;
+    const double *bp = knots + (k - 1);
+    double x0[64], w0[64], x[64], w[64];
+    or_gauss_legendre(k_GL, x0, w0);
+    double complex *R = (double complex *)r_mat, *D = (double complex *)dr_mat,
+                   *Ri = (double complex *)r_inv_mat;
+    if (R) memset(R, 0, sizeof(double complex) * (size_t)nb * nb);
+    if (D) memset(D, 0, sizeof(double complex) * (size_t)nb * nb);
+    if (Ri) memset(Ri, 0, sizeof(double complex) * (size_t)nb * nb);
+    for (int64_t jb = 1; jb <= nb; ++jb)
+        for (int64_t ib = 1; ib <= nb; ++ib) {
+            if (llabs(jb - ib) >= k) continue;
+            for (int64_t ir = 1; ir <= n_iv; ++ir) {
+                if (!(supp(ir, ib + 1, k) && supp(ir, jb + 1, k))) continue;
+                gl_interval(k_GL, x0, w0, bp[ir - 1], bp[ir], x, w);
+                size_t o = (size_t)(jb - 1) * nb + (ib - 1);
+                for (int64_t s = 0; s < k_GL; ++s) {
+                    double Bi = or_bvalue(knots, n, k, x[s], 0, ir, ib + 1);
+                    double Bj = or_bvalue(knots, n, k, x[s], 0, ir, jb + 1);
+                    if (gauge == 0) {
+                        /* compute_radial_dip_len (mat_els.f90:348-367) */
+                        R[o] = R[o] + w[s] * x[s] * Bi * Bj;
+                    } else {
+                        /* compute_radial_dip_vel (mat_els.f90:369-390) */
+                        double DBj = or_bvalue(knots, n, k, x[s], 1, ir, jb + 1);
+                        D[o] = D[o] + (-I) * w[s] * Bi * DBj;
+                        Ri[o] = Ri[o] + (-I) * w[s] * Bi * Bj / x[s];
+                    }
+                }
+            }
+        }
+}
+
+/* ang_dip_red (mat_els.f90:811-828) */
+static double ang_dip_red(int64_t L1, int64_t L2, int64_t la, int64_t lb, int64_t lc, int64_t ld) {
+    double res = 0.0;
+    if (lb == ld) res = res + fabs(or_six_j(L1, 1, L2, lc, lb, la) * or_C_red_mat(1, la, lc));
+    if (la == lc) res = res + fabs(or_six_j(L1, 1, L2, ld, la, lb) * or_C_red_mat(1, lb, ld));
+    return res;
+}
+
+/* dip_red_1p_len / dip_red_1p_vel (mat_els.f90:772-809) for (n, n_p, l, l_p) */
+static double complex dip_red_1p(int64_t gauge, int64_t n, int64_t np, int64_t l, int64_t lp,
+                                 int64_t nb, const double complex *R, const double complex *D,
+                                 const double complex *Ri) {
+    size_t o = (size_t)(np - 1) * nb + (n - 1);
+    if (gauge == 0) return R[o] * or_C_red_mat(1, l, lp);
+    if (llabs(l - lp) != 1) return 0.0;
+    if (l > lp) return sqrt((double)l) * (D[o] - (double)(lp + 1) * Ri[o]);
+    return -sqrt((double)lp) * (D[o] + (double)lp * Ri[o]);
+}
+
+/* dip_red_mat (mat_els.f90:739-770); confs(1) = (na,nb1; la,lb), confs(2) = (nc,nd; lc,ld) */
+static double complex dip_red_mat(int64_t L1, int64_t L2, int64_t na, int64_t nb1, int64_t la,
+                                  int64_t lb, int64_t nc, int64_t nd, int64_t lc, int64_t ld,
+                                  int64_t gauge, int64_t nbas, const double complex *S,
+                                  const double complex *R, const double complex *D,
+                                  const double complex *Ri) {
+    double complex r1 = 0.0, r2 = 0.0;
+    double sq = sqrt((double)((2 * L1 + 1) * (2 * L2 + 1)));
+    if (lb == ld) {
+        double sg = ((la + lb + L2 + 1) & 1) ? -1.0 : 1.0;
+        r1 = sg * sq * or_six_j(L1, 1, L2, lc, lb, la) *
+             dip_red_1p(gauge, na, nc, la, lc, nbas, R, D, Ri) * S[(size_t)(nd - 1) * nbas + (nb1 - 1)];
+    }
+    if (la == lc) {
+        double sg = ((la + ld + L1 + 1) & 1) ? -1.0 : 1.0;
+        r2 = sg * sq * or_six_j(L1, 1, L2, ld, la, lb) *
+             dip_red_1p(gauge, nb1, nd, lb, ld, nbas, R, D, Ri) * S[(size_t)(nc - 1) * nbas + (na - 1)];
+    }
+    return r1 + r2;
+}
+
+int64_t or_dip_block(const or_config *rows, int64_t n_rows, int64_t L1, int64_t M1, int64_t pi1,
+                     const or_config *cols, int64_t n_cols, int64_t L2, int64_t M2, int64_t pi2,
+                     int64_t q, int64_t compute, int64_t k, int64_t n_b, int64_t gauge,
+                     const double *S, const double *r_mat, const double *dr_mat,
+                     const double *r_inv_mat, int64_t *ptr, int64_t *idx, double *data) {
+    const double complex *Sc = (const double complex *)S, *R = (const double complex *)r_mat,
+                         *D = (const double complex *)dr_mat, *Ri = (const double complex *)r_inv_mat;
+    int parity_allowed = (pi1 != 0) != (pi2 != 0);
+    double ang = (((L1 - M1) & 1) ? -1.0 : 1.0) * or_three_j(L1, 1, L2, -M1, q, M2);
+    if (fabs(ang) < 5e-16 || !parity_allowed || !compute) {
+        if (ptr)
+            for (int64_t i = 0; i <= n_rows; ++i) ptr[i] = 1;
+        return 0;
+    }
+    int64_t p = 1;
+    if (ptr) ptr[0] = 1;
+    for (int64_t i = 0; i < n_rows; ++i) {
+        int64_t na = rows[i].n1, nb1 = rows[i].n2, la = rows[i].l1, lb = rows[i].l2;
+        for (int64_t j = 0; j < n_cols; ++j) {
+            int64_t nc = cols[j].n1, nd = cols[j].n2, lc = cols[j].l1, ld = cols[j].l2;
+            int support = llabs(na - nc) < k && llabs(nb1 - nd) < k;
+            int support_ex = llabs(na - nd) < k && llabs(nb1 - nc) < k;
+            int nz = 0;
+            if (support) {
+                if (ang_dip_red(L1, L2, la, lb, lc, ld) > 5e-16) nz = 1;
+            } else if (support_ex) {
+                if (ang_dip_red(L1, L2, la, lb, lc, ld) > 5e-16) nz = 1;
+            }
+            if (!nz) continue;
+            if (idx) {
+                /* dip_mat_neq (mat_els.f90:717-737) */
+                double complex red = dip_red_mat(L1, L2, na, nb1, la, lb, nc, nd, lc, ld, gauge, n_b,
+                                                 Sc, R, D, Ri);
+                double complex red_ex = dip_red_mat(L1, L2, na, nb1, la, lb, nd, nc, ld, lc, gauge,
+                                                    n_b, Sc, R, D, Ri);
+                double sg = ((L2 + lc + ld) & 1) ? -1.0 : 1.0;
+                double complex v = ang * (red + sg * red_ex);
+                idx[p - 1] = j + 1;
+                data[2 * (p - 1)] = creal(v);
+                data[2 * (p - 1) + 1] = cimag(v);
+            }
+            p++;
+        }
+        if (ptr) ptr[i + 1] = p;
+    }
+    return p - 1;
+}

@@ -93,6 +93,22 @@ void or_setup_H1p(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
                   int64_t l, int64_t cap_order, double cap_r0, double cap_eta_re,
                   double cap_eta_im, double *H);
 
+/* setup_radial_dip (src/mat_els/mat_els.f90:120-170, 348-390): gauge 0 = length
+ * ('l': r_mat), 1 = velocity ('v': dr_mat, r_inv_mat).  Complex n_b x n_b
+ * column-major; unused outputs may be NULL. */
+void or_setup_radial_dip(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL,
+                         int64_t gauge, double *r_mat, double *dr_mat, double *r_inv_mat);
+
+/* construct_dip_block_tensor with init_dip_block (src/mat_els/dipole.f90:8-47,
+ * 87-146) for the block (row symmetry (L1, M1, pi1), column symmetry (L2, M2,
+ * pi2)) and polarisation q; compute = 0 gives the empty block as the reference
+ * does for skipped pairs.  Pass NULL outputs to count only (nnz returned). */
+int64_t or_dip_block(const or_config *rows, int64_t n_rows, int64_t L1, int64_t M1, int64_t pi1,
+                     const or_config *cols, int64_t n_cols, int64_t L2, int64_t M2, int64_t pi2,
+                     int64_t q, int64_t compute, int64_t k, int64_t n_b, int64_t gauge,
+                     const double *S, const double *r_mat, const double *dr_mat,
+                     const double *r_inv_mat, int64_t *ptr, int64_t *idx, double *data);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,6 +51,9 @@ def lib():
                                       i64, p, p, p, p, p, p, p, p]),
         "or_setup_S": (None, [p, i64, i64, i64, p]),
         "or_setup_H1p": (None, [p, i64, i64, i64, i64, i64, i64, dbl, dbl, dbl, p]),
+        "or_setup_radial_dip": (None, [p, i64, i64, i64, i64, p, p, p]),
+        "or_dip_block": (i64, [p, i64, i64, i64, i64, p, i64, i64, i64, i64, i64, i64, i64, i64,
+                               i64, p, p, p, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -185,3 +188,30 @@ def setup_H1p(knots, k, k_GL, Z, n_l, cap_order=2, cap_r0=10.0, cap_eta=1e-3 + 0
                            eta.imag, _p(Hl))
         H[:, :, l] = Hl
     return H
+
+
+def setup_radial_dip(knots, k, k_GL, gauge):
+    """(r_mat,) for the length gauge, (dr_mat, r_inv_mat) for the velocity gauge."""
+    t = np.ascontiguousarray(knots, dtype=np.float64)
+    nb = t.size - k - 2
+    mk = lambda: np.zeros((nb, nb), dtype=np.complex128, order="F")
+    r, d, ri = mk(), mk(), mk()
+    lib().or_setup_radial_dip(_p(t), t.size, k, k_GL, int(gauge), _p(r), _p(d), _p(ri))
+    return (r,) if gauge == 0 else (d, ri)
+
+
+def dip_block(rows, sym1, cols, sym2, q, compute, k, n_b, gauge, S, mats):
+    """construct_dip_block_tensor for one pair of symmetries; mats as returned
+    by setup_radial_dip."""
+    rows, cols = np.ascontiguousarray(rows), np.ascontiguousarray(cols)
+    S = np.asfortranarray(S, dtype=np.complex128)
+    r = mats[0] if gauge == 0 else None
+    d, ri = (mats[0], mats[1]) if gauge == 1 else (None, None)
+    a = [_p(rows), rows.size, *[int(x) for x in sym1], _p(cols), cols.size,
+         *[int(x) for x in sym2], int(q), int(bool(compute)), k, n_b, int(gauge), _p(S), _p(r),
+         _p(d), _p(ri)]
+    n = lib().or_dip_block(*a, None, None, None)
+    D = dict(index_ptr=np.zeros(rows.size + 1, np.int64), indices=np.zeros(n, np.int64),
+             data=np.zeros(n, np.complex128), nnz=n)
+    lib().or_dip_block(*a, _p(D["index_ptr"]), _p(D["indices"]), _p(D["data"]))
+    return D

@@ -205,3 +205,65 @@ def test_mixed_blocks_match_oracle(bs2e, oracle, case):
             rel = np.abs(Hg["data"] - Hr["data"]) / np.maximum(Hr["scale"], 1e-300)
             worst = max(worst, float(rel.max()) if rel.size else 0.0)
     print("mixed %s: max error / term scale = %.3e" % (case, worst))
+
+
+# ---------------------------------------------------------------------------
+# Dipole blocks (construct_dip_block_tensor, src/mat_els/dipole.f90:8-146)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("gauge", [0, 1])
+def test_radial_dipole_matches_oracle(bs2e, oracle, gauge):
+    c = CASES["small2"]
+    t = knots(bs2e, "small2")
+    want = oracle.setup_radial_dip(t, c["k"], c["q"], gauge)
+    with _handle(bs2e, "small2") as h:
+        got = h.radial_dipole(gauge)
+    for g, w in zip(got, want):
+        np.testing.assert_allclose(g, w, rtol=0, atol=1e-13 * np.abs(w).max())
+
+
+@pytest.mark.parametrize("case", ["small2", "cut"])
+@pytest.mark.parametrize("gauge", [0, 1])
+def test_dipole_blocks_match_oracle(bs2e, oracle, case, gauge):
+    c = CASES[case]
+    ref = oracle_reference(case)
+    mats = oracle.setup_radial_dip(ref["knots"], c["k"], c["q"], gauge)
+    bl = [b for b in blocks(bs2e, case) if b[3] == 0]
+    n_checked = 0
+    with _handle(bs2e, case) as h:
+        h.set_one_body(ref["H1p"], ref["S"])
+        if gauge == 0:
+            h.set_radial_dipole(0, r_mat=mats[0])
+        else:
+            h.set_radial_dipole(1, dr_mat=mats[0], r_inv_mat=mats[1])
+        for q in (-1, 0, 1):
+            for j, (L2, M2, p2, _, cols) in enumerate(bl):
+                for i, (L1, M1, p1, _, rows) in enumerate(bl):
+                    compute = not (i > j and case == "cut")  # full=.false. skips i > j
+                    want = oracle.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), q, compute,
+                                            c["k"], c["n_b"], gauge, ref["S"], mats)
+                    got = h.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), q, compute)
+                    assert got["nnz"] == want["nnz"]
+                    np.testing.assert_array_equal(got["index_ptr"], want["index_ptr"])
+                    np.testing.assert_array_equal(got["indices"], want["indices"])
+                    scale = max(np.abs(want["data"]).max() if want["nnz"] else 0.0, 1e-300)
+                    np.testing.assert_allclose(got["data"], want["data"], rtol=0,
+                                               atol=1e-12 * scale)
+                    n_checked += want["nnz"] > 0
+    assert n_checked > 0
+
+
+def test_device_radial_dipole_drives_blocks(bs2e, oracle):
+    c = CASES["small2"]
+    ref = oracle_reference("small2")
+    mats = oracle.setup_radial_dip(ref["knots"], c["k"], c["q"], 1)
+    bl = [b for b in blocks(bs2e, "small2") if b[3] == 0]
+    (L1, M1, p1, _, rows), (L2, M2, p2, _, cols) = bl[0], bl[1]
+    with _handle(bs2e, "small2") as h:
+        h.set_one_body(ref["H1p"], ref["S"])
+        h.radial_dipole(1, copy_out=False)
+        got = h.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), 0)
+    want = oracle.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), 0, True, c["k"], c["n_b"], 1,
+                            ref["S"], mats)
+    np.testing.assert_array_equal(got["indices"], want["indices"])
+    np.testing.assert_allclose(got["data"], want["data"], rtol=0,
+                               atol=1e-12 * np.abs(want["data"]).max())
