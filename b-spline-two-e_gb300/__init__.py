@@ -41,6 +41,7 @@ EXPORTS = [
     "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_configs", "bs2e_ang_k_LS",
     "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
     "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
+    "bs2e_rk_get_batch_static",
 ]
 
 
@@ -79,6 +80,7 @@ def lib():
         "bs2e_rk": (st, [p, i64, i64]),
         "bs2e_rk_get": (st, [p, p, p]),
         "bs2e_rk_get_batch": (st, [p, i64, p, p]),
+        "bs2e_rk_get_batch_static": (st, [p, i64, p, p]),
         "bs2e_set_one_body": (st, [p, p, i64, p]),
         "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
         "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
@@ -225,6 +227,15 @@ class Bs2e:
         keys = np.ascontiguousarray(keys, dtype=np.int64).reshape(-1, 4)
         vals = np.zeros((keys.shape[0], self.K1))
         _check(self._h, lib().bs2e_rk_get_batch(self._h, keys.shape[0], _ptr(keys), _ptr(vals)))
+        return vals
+
+    def rk_get_static(self, keys):
+        """rk_get through the allocation-free entry point (at most 4096 keys;
+        see bs2e_rk_get_batch_static in include/bs2e.h)."""
+        keys = np.ascontiguousarray(keys, dtype=np.int64).reshape(-1, 4)
+        vals = np.zeros((keys.shape[0], self.K1))
+        _check(self._h, lib().bs2e_rk_get_batch_static(self._h, keys.shape[0], _ptr(keys),
+                                                       _ptr(vals)))
         return vals
 
     # -- one-body matrices ---------------------------------------------------

@@ -120,6 +120,20 @@ BS2E_API bs2e_status bs2e_rk_get(bs2e_handle *h, const int64_t key[4], double *v
 BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t *keys,
                                        double *vals);
 
+/* bs2e_rk_get_batch without any device allocation.  This entry point has no
+ * counterpart in the reference.  It is for callers that can't allocate device
+ * memory at lookup time: a caller that has filled HBM with CSR blocks can't
+ * risk an allocation failing, and the cudaFree of the allocating lookup waits
+ * for the whole device, stalling work on other streams.  Keys and values are
+ * staged in one file-scope device array of at most 4096 keys (1.125 MiB on
+ * every GPU that loads the library, held until the process exits); larger n
+ * is rejected with BS2E_ERR_ARG.  The first call on a device looks up the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture on that device.  All calls on a device share the array, which keeps
+ * the last call's contents; calls whose GPU work overlaps race on it. */
+BS2E_API bs2e_status bs2e_rk_get_batch_static(bs2e_handle *h, int64_t n, const int64_t *keys,
+                                              double *vals);
+
 /* Uploads the one-body matrices used by every block: H1p is n_b x n_b x n_l
  * complex (H_vec(l)%data for l = 0..n_l-1, main_basis_setup.f90:95-99), S is
  * n_b x n_b complex (main_basis_setup.f90:91-93). */
