@@ -41,7 +41,7 @@ EXPORTS = [
     "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_configs", "bs2e_ang_k_LS",
     "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
     "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
-    "bs2e_rk_get_batch_static",
+    "bs2e_rk_get_batch_static", "bs2e_write_block_diag", "bs2e_write_block",
 ]
 
 
@@ -81,6 +81,8 @@ def lib():
         "bs2e_rk_get": (st, [p, p, p]),
         "bs2e_rk_get_batch": (st, [p, i64, p, p]),
         "bs2e_rk_get_batch_static": (st, [p, i64, p, p]),
+        "bs2e_write_block_diag": (st, [ctypes.c_char_p, i64, p, p, p, p, p, i64]),
+        "bs2e_write_block": (st, [ctypes.c_char_p, i64, i64, p, p, p, p, p, i64]),
         "bs2e_set_one_body": (st, [p, p, i64, p]),
         "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
         "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
@@ -150,6 +152,42 @@ def three_j(ja, jb, jc, ma, mb, mc):
 
 def six_j(ja, jb, jc, jd, je, jf):
     return lib().bs2e_six_j(ja, jb, jc, jd, je, jf)
+
+
+def _block_arrays(blocks):
+    n = len(blocks)
+    shapes = np.zeros((n, 2), dtype=np.int64)
+    nnz = np.zeros(n, dtype=np.int64)
+    P = (ctypes.c_void_p * max(n, 1))()
+    I = (ctypes.c_void_p * max(n, 1))()
+    D = (ctypes.c_void_p * max(n, 1))()
+    keep = []
+    for i, b in enumerate(blocks):
+        shapes[i] = b["shape"]
+        nnz[i] = b["nnz"]
+        if b["nnz"] > 0:
+            arrs = (np.ascontiguousarray(b["index_ptr"], dtype=np.int64),
+                    np.ascontiguousarray(b["indices"], dtype=np.int64),
+                    np.ascontiguousarray(b["data"], dtype=np.complex128))
+            keep.append(arrs)
+            P[i], I[i], D[i] = (a.ctypes.data for a in arrs)
+    return shapes, nnz, P, I, D, keep
+
+
+def write_block_diag(path, blocks, max_subrecord=0):
+    """H_diag.dat / S_diag.dat (CS_block_diag_store, block_tools.f90:458-485):
+    blocks is a list of dicts with shape, nnz, index_ptr, indices, data."""
+    shapes, nnz, P, I, D, keep = _block_arrays(blocks)
+    _check(None, lib().bs2e_write_block_diag(os.fsencode(path), len(blocks), _ptr(shapes),
+                                             _ptr(nnz), P, I, D, int(max_subrecord)))
+
+
+def write_block(path, blocks, n_rows_b, n_cols_b, max_subrecord=0):
+    """D_q.dat (CS_block_store, block_tools.f90:386-415): blocks[(i, j)]."""
+    order = [blocks[(i, j)] for j in range(n_cols_b) for i in range(n_rows_b)]
+    shapes, nnz, P, I, D, keep = _block_arrays(order)
+    _check(None, lib().bs2e_write_block(os.fsencode(path), n_rows_b, n_cols_b, _ptr(shapes),
+                                        _ptr(nnz), P, I, D, int(max_subrecord)))
 
 
 def _check(h, status):

@@ -462,8 +462,17 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
     return ff_add(a, FF{__fmul_rn(b.s, sc), __fmul_rn(b.c, sc)});
 }
 
+// Minimum resident CTAs per SM the fill kernel is compiled for (caps its
+// registers at 65536 / (128 * this)).  Measured on config 2 (fill time per
+// step, FP64 / mixed): 8 -> 39.2 / 42.7 ms (64 registers), 6 -> 40.3 / 45.9,
+// 4 -> 46.8 / 50.7; the kernel is bound by the FP64 pipe (plain) and the
+// integer ALU pipe (mixed), not by occupancy.
+#ifndef BS2E_FILL_MIN_BLOCKS
+#define BS2E_FILL_MIN_BLOCKS 8
+#endif
+
 template <bool MIXED>
-__global__ void __launch_bounds__(128) k_csr_fill(FillArgs F) {
+__global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
     __shared__ int sexp[kMaxK1];

@@ -230,6 +230,28 @@ BS2E_API bs2e_status bs2e_dip_block_fill(bs2e_handle *h, const bs2e_config *rows
                                          int64_t *index_ptr, int64_t *indices, double *data,
                                          int64_t out_on_device);
 
+/* Writers of the reference's block CSR files in gfortran's unformatted
+ * sequential format (4-byte record markers; records above 2147483639 bytes
+ * split into subrecords with signed markers).
+ * bs2e_write_block_diag writes a block_diag_CS as CS_block_diag_store does
+ * (src/tools/block_tools.f90:458-485) -- H_diag.dat / S_diag.dat: n_blocks
+ * diagonal blocks, shapes[2*i..2*i+1] = (rows, cols), nnz[i], and per block
+ * the 1-based CSR arrays (index_ptr[i] rows+1, indices[i] nnz, data[i] nnz
+ * complex128; ignored when nnz[i] = 0).
+ * bs2e_write_block writes a block_CS as CS_block_store does (:386-415) --
+ * D_q.dat: n_rows_b x n_cols_b blocks, block (i, j) at index i + n_rows_b*j.
+ * max_subrecord <= 0 uses gfortran's default subrecord size. */
+BS2E_API bs2e_status bs2e_write_block_diag(const char *path, int64_t n_blocks,
+                                           const int64_t *shapes, const int64_t *nnz,
+                                           const int64_t *const *index_ptr,
+                                           const int64_t *const *indices,
+                                           const double *const *data, int64_t max_subrecord);
+BS2E_API bs2e_status bs2e_write_block(const char *path, int64_t n_rows_b, int64_t n_cols_b,
+                                      const int64_t *shapes, const int64_t *nnz,
+                                      const int64_t *const *index_ptr,
+                                      const int64_t *const *indices, const double *const *data,
+                                      int64_t max_subrecord);
+
 /* The CUDA stream all work of the handle runs on (cudaStream_t as void*), the
  * number of kernels the handle has launched so far, and a full synchronize. */
 BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream);
