@@ -42,6 +42,9 @@ EXPORTS = [
     "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
     "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
     "bs2e_rk_get_batch_static", "bs2e_write_block_diag", "bs2e_write_block",
+    "bs2e_csr_mv", "bs2e_block_count_rows", "bs2e_block_fill_rows", "bs2e_rk_export",
+    "bs2e_batch_create", "bs2e_batch_run", "bs2e_batch_tuning", "bs2e_batch_destroy",
+    "bs2e_csr_from_blocks",
 ]
 
 
@@ -53,7 +56,7 @@ class Bs2eError(RuntimeError):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int64), ("device", ctypes.c_int64),
-                ("reserved", ctypes.c_int64 * 6)]
+                ("stage_bytes", ctypes.c_int64), ("reserved", ctypes.c_int64 * 5)]
 
 
 _lib = None
@@ -83,6 +86,15 @@ def lib():
         "bs2e_rk_get_batch_static": (st, [p, i64, p, p]),
         "bs2e_write_block_diag": (st, [ctypes.c_char_p, i64, p, p, p, p, p, i64]),
         "bs2e_write_block": (st, [ctypes.c_char_p, i64, i64, p, p, p, p, p, i64]),
+        "bs2e_csr_mv": (st, [p, i64, i64, i64, i64, p, p, p, p, p, i64]),
+        "bs2e_rk_export": (st, [p, i64, p, i64]),
+        "bs2e_batch_create": (st, [p, i64, p]),
+        "bs2e_batch_run": (st, [p]),
+        "bs2e_batch_tuning": (st, [p, p, p, p, p]),
+        "bs2e_batch_destroy": (st, [p]),
+        "bs2e_csr_from_blocks": (st, [p, i64, i64, p, p, p, p, p, p, p, p, i64]),
+        "bs2e_block_count_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p]),
+        "bs2e_block_fill_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, i64]),
         "bs2e_set_one_body": (st, [p, p, i64, p]),
         "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
         "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
@@ -203,7 +215,7 @@ def _check(h, status):
 class Bs2e:
     """One B-spline basis on one GPU (wraps a bs2e_handle)."""
 
-    def __init__(self, knots, k, k_GL, max_k, precision=PREC_FP64, device=0):
+    def __init__(self, knots, k, k_GL, max_k, precision=PREC_FP64, device=0, stage_bytes=0):
         L_ = lib()
         self.knots = np.ascontiguousarray(knots, dtype=np.float64)
         self.k, self.k_GL, self.max_k = int(k), int(k_GL), int(max_k)
@@ -212,6 +224,7 @@ class Bs2e:
         L_.bs2e_default_opts(ctypes.byref(opts))
         opts.precision = int(precision)
         opts.device = int(device)
+        opts.stage_bytes = int(stage_bytes)
         h = ctypes.c_void_p()
         st = L_.bs2e_create(_ptr(self.knots), self.knots.size, self.k, self.k_GL, self.max_k,
                             ctypes.byref(opts), ctypes.byref(h))
@@ -314,6 +327,43 @@ class Bs2e:
         self.block_fill_into(cf, L, full, spin, H, S, on_device=False)
         return H, S
 
+    def block_rows(self, cf, L, row_first, row_count, full=True, spin=0):
+        """Rows [row_first, row_first + row_count) of a block into host arrays:
+        (H, S) dicts with a range-local 1-based index_ptr."""
+        cf = as_configs(cf)
+        nh, ns = ctypes.c_int64(), ctypes.c_int64()
+        a = [self._h, _ptr(cf), cf.size, int(L), int(spin), int(bool(full)), int(row_first),
+             int(row_count)]
+        _check(self._h, lib().bs2e_block_count_rows(*a, ctypes.byref(nh), ctypes.byref(ns)))
+        n = int(row_count)
+        H = dict(shape=(n, cf.size), nnz=nh.value, index_ptr=np.zeros(n + 1, np.int64),
+                 indices=np.zeros(nh.value, np.int64), data=np.zeros(nh.value, np.complex128))
+        S = dict(shape=(n, cf.size), nnz=ns.value, index_ptr=np.zeros(n + 1, np.int64),
+                 indices=np.zeros(ns.value, np.int64), data=np.zeros(ns.value, np.complex128))
+        _check(self._h, lib().bs2e_block_fill_rows(*a, *[_ptr(H[x]) for x in
+                                                         ("index_ptr", "indices", "data")],
+                                                   *[_ptr(S[x]) for x in
+                                                     ("index_ptr", "indices", "data")], 0))
+        return H, S
+
+    def block_rows_into(self, cf, L, row_first, row_count, full, spin, H, S):
+        """Rows of a block into device buffers (dicts of integer device addresses)."""
+        cf = as_configs(cf)
+        args = [ctypes.c_void_p(int(H[x])) for x in ("index_ptr", "indices", "data")]
+        args += [ctypes.c_void_p(int(S[x])) for x in ("index_ptr", "indices", "data")]
+        _check(self._h, lib().bs2e_block_fill_rows(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                   int(bool(full)), int(row_first),
+                                                   int(row_count), *args, 1))
+
+    def block_count_rows(self, cf, L, row_first, row_count, full=True, spin=0):
+        cf = as_configs(cf)
+        nh, ns = ctypes.c_int64(), ctypes.c_int64()
+        _check(self._h, lib().bs2e_block_count_rows(self._h, _ptr(cf), cf.size, int(L),
+                                                    int(spin), int(bool(full)), int(row_first),
+                                                    int(row_count), ctypes.byref(nh),
+                                                    ctypes.byref(ns)))
+        return nh.value, ns.value
+
     def block_fill_into(self, cf, L, full, spin, H, S, on_device=False):
         """Fills caller-provided arrays: numpy (host) or, with on_device, integer
         device addresses in the dicts' 'index_ptr', 'indices', 'data' entries."""
@@ -359,6 +409,67 @@ class Bs2e:
                                                   _ptr(D["indices"]), _ptr(D["data"]), 0))
         return D
 
+    def rk_export(self, k, out=None, on_device=False):
+        """Multipole k of the store as an (N, N, W, W) array (host), or into the
+        device address `out` with on_device."""
+        W = 2 * self.k - 1
+        if on_device:
+            _check(self._h, lib().bs2e_rk_export(self._h, int(k), ctypes.c_void_p(int(out)), 1))
+            return out
+        if out is None:
+            out = np.zeros((self.n_b, self.n_b, W, W))
+        _check(self._h, lib().bs2e_rk_export(self._h, int(k), _ptr(out), 0))
+        return out
+
+    # -- mat-vec -------------------------------------------------------------
+    def csr_mv(self, A, x, op=0, y=None):
+        """CSR_mv (op 0), CSR_T_mv (op 1) or CSR_mv_sym (op 2) of a CSR dict
+        (shape, nnz, index_ptr, indices, data) with x (host arrays)."""
+        n_rows, n_cols = A["shape"]
+        nnz = int(A["nnz"])
+        ptr = np.ascontiguousarray(A["index_ptr"], dtype=np.int64)
+        idx = np.ascontiguousarray(A["indices"], dtype=np.int64) if nnz else None
+        dat = np.ascontiguousarray(A["data"], dtype=np.complex128) if nnz else None
+        xv = np.ascontiguousarray(x, dtype=np.complex128)
+        n_in, n_out = (n_rows, n_cols) if op == 1 else (n_cols, n_rows)
+        if xv.size != n_in:
+            raise ValueError("x has %d entries, the product needs %d" % (xv.size, n_in))
+        if y is None:
+            y = np.zeros(n_out, dtype=np.complex128)
+        _check(self._h, lib().bs2e_csr_mv(self._h, int(op), n_rows, n_cols, nnz, _ptr(ptr),
+                                          _ptr(idx), _ptr(dat), _ptr(xv), _ptr(y), 0))
+        return y
+
+    def csr_from_blocks(self, blocks, n_rb, n_cb):
+        """CSR_from_block of host CSR dicts blocks[(i, j)] (shape, nnz and,
+        when nnz > 0, index_ptr / indices / data); returns one CSR dict."""
+        order = [blocks[(i, j)] for j in range(n_cb) for i in range(n_rb)]
+        shapes, nnz, P, I, D, keep = _block_arrays(order)
+        rows = sum(int(blocks[(i, 0)]["shape"][0]) for i in range(n_rb))
+        cols = sum(int(blocks[(0, j)]["shape"][1]) for j in range(n_cb))
+        tot = int(nnz.sum())
+        out = dict(shape=(rows, cols), nnz=tot, index_ptr=np.zeros(rows + 1, np.int64),
+                   indices=np.zeros(tot, np.int64), data=np.zeros(tot, np.complex128))
+        _check(self._h, lib().bs2e_csr_from_blocks(self._h, n_rb, n_cb, _ptr(shapes), _ptr(nnz),
+                                                   P, I, D, _ptr(out["index_ptr"]),
+                                                   _ptr(out["indices"]), _ptr(out["data"]), 0))
+        return out
+
+    def csr_from_block_diag(self, blocks):
+        """CSR_from_block_diag: the diagonal blocks joined into one CSR."""
+        n = len(blocks)
+        grid = {}
+        for i in range(n):
+            for j in range(n):
+                grid[(i, j)] = blocks[i] if i == j else dict(
+                    shape=(blocks[i]["shape"][0], blocks[j]["shape"][1]), nnz=0)
+        return self.csr_from_blocks(grid, n, n)
+
+    def csr_mv_device(self, op, n_rows, n_cols, nnz, ptr, idx, data, x, y):
+        """The same product on device pointers (ints), e.g. torch tensors' data_ptr()."""
+        _check(self._h, lib().bs2e_csr_mv(self._h, int(op), n_rows, n_cols, nnz, ptr, idx, data,
+                                          x, y, 1))
+
     # -- plumbing ------------------------------------------------------------
     @property
     def stream(self):
@@ -374,3 +485,38 @@ class Bs2e:
 
     def synchronize(self):
         _check(self._h, lib().bs2e_synchronize(self._h))
+
+
+class RadialBatch:
+    """bs2e_slater + bs2e_rk of many Bs2e handles as one batched, graph-captured
+    radial stage (bs2e_batch_*).  The handles must outlive the batch."""
+
+    def __init__(self, handles):
+        self.handles = list(handles)
+        arr = (ctypes.c_void_p * len(self.handles))(*[h._h.value for h in self.handles])
+        b = ctypes.c_void_p()
+        _check(self.handles[0]._h, lib().bs2e_batch_create(arr, len(self.handles), ctypes.byref(b)))
+        self._b = b
+
+    def run(self):
+        _check(self.handles[0]._h, lib().bs2e_batch_run(self._b))
+
+    def tuning(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        lib().bs2e_batch_tuning(self._b, *[ctypes.byref(x) for x in v])
+        return dict(rk_threads=v[0].value, chunk=v[1].value, graph=bool(v[2].value),
+                    launches=v[3].value)
+
+    def close(self):
+        if getattr(self, "_b", None):
+            lib().bs2e_batch_destroy(self._b)
+            self._b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        self.close()

@@ -15,7 +15,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbs2e.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 SOURCES = ["bs2e_capi.cu", "bs2e_radial.cu", "bs2e_assembly.cu", "bs2e_dipole.cu",
-           "bs2e_noalloc.cu", "bs2e_angular.cpp", "bs2e_basis.cpp", "bs2e_fortio.cpp"]
+           "bs2e_noalloc.cu", "bs2e_angular.cpp", "bs2e_basis.cpp", "bs2e_fortio.cpp",
+           "bs2e_spmv.cu", "bs2e_batch.cu", "bs2e_blockcsr.cu"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(HERE, "..", "include")]
 

@@ -285,7 +285,11 @@ struct FillArgs {
     const float4 *Hbf, *Sbf;  // the same bands as FP32 pairs (re hi, re lo, im hi, im lo)
     int s_real;
     int ff_one_body;          // 1: mixed path may use Hbf/Sbf (S real, magnitudes in range)
-    const int64_t *Hptr, *Sptr;  // 1-based CSR pointers of the block
+    // rows [row0, row1) are filled; row r starts at output position
+    // Hptr[r - ptr_row0] - 1 - Hbase (likewise S), 1-based CSR pointers
+    const int64_t *Hptr, *Sptr;
+    int64_t row0, row1, ptr_row0, Hbase, Sbase;
+    int a0;  // tile (n_a, n_b) of CTA x: n_a = a0 + x / N, n_b = x % N + 1
     int64_t *Hidx, *Sidx;
     double2 *Hdat, *Sdat;
     int *err;
@@ -480,17 +484,18 @@ __global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs
     __shared__ int sKo[4][2][kMaxK1];
     __shared__ int srow[kMaxCh], sch[kMaxCh], snrow;
     const BlockArgs &A = F.B;
-    const int n_a = blockIdx.x / A.N + 1, n_b = blockIdx.x % A.N + 1;
-    const size_t tix = (size_t)blockIdx.x;
+    const int n_a = F.a0 + (int)(blockIdx.x / A.N), n_b = blockIdx.x % A.N + 1;
+    const size_t tix = (size_t)(n_a - 1) * A.N + (n_b - 1);
     // rows of this tile: one per channel whose (n1 = n_a) group holds n2 = n_b
     if (threadIdx.x == 0) snrow = 0;
     __syncthreads();
     for (int c = threadIdx.x; c < A.n_ch; c += blockDim.x) {
         size_t s = (size_t)c * A.segS + n_a;
         int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
-        if (base >= 0 && lo <= n_b && n_b <= hi) {
+        const int64_t row = base + (n_b - lo);
+        if (base >= 0 && lo <= n_b && n_b <= hi && row >= F.row0 && row < F.row1) {
             int slot = atomicAdd(&snrow, 1);
-            srow[slot] = base + (n_b - lo);
+            srow[slot] = (int)row;
             sch[slot] = c;
         }
     }
@@ -517,7 +522,8 @@ __global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs
         const float4 *HbB = F.Hbf ? F.Hbf + (size_t)l_b * A.N * W + rb : nullptr;  // H_lb[n_b][.]
         const float4 *SA = F.Sbf ? F.Sbf + ra : nullptr;                           // S[n_a][.]
         const float4 *SB = F.Sbf ? F.Sbf + rb : nullptr;                           // S[n_b][.]
-        int64_t oH = F.Hptr[row] - 1, oS = F.Sptr[row] - 1;
+        int64_t oH = F.Hptr[row - F.ptr_row0] - 1 - F.Hbase;
+        int64_t oS = F.Sptr[row - F.ptr_row0] - 1 - F.Sbase;
         for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
             const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
             const int flags = pi.flags;
@@ -862,17 +868,18 @@ void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64
     h->launches += 3;
 }
 
-void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr) {
-    int64_t n = h->plan.n_config;
+void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr, int64_t row0,
+                       int64_t n) {
     int64_t *part = h->blk.scan_tmp;
-    scan_one(h, h->blk.cntH, n, part, d_Hptr);
-    scan_one(h, h->blk.cntS, n, part, d_Sptr);
+    scan_one(h, h->blk.cntH + row0, n, part, d_Hptr);
+    scan_one(h, h->blk.cntS + row0, n, part, d_Sptr);
 }
 
 size_t fill_smem(const Radial &g) { return (size_t)g.tile * sizeof(double); }
 
-void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_Sptr,
-                       int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx, double2 *d_Sdat) {
+void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr,
+                       const int64_t *d_Sptr, int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx,
+                       double2 *d_Sdat) {
     FillArgs F;
     F.B = block_args(h);
     F.R = h->d_R;
@@ -892,9 +899,15 @@ void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_S
     F.Hdat = d_Hdat;
     F.Sdat = d_Sdat;
     F.err = h->d_err;
+    F.row0 = r.row0;
+    F.row1 = r.row1;
+    F.ptr_row0 = r.ptr_row0;
+    F.Hbase = r.Hbase;
+    F.Sbase = r.Sbase;
+    F.a0 = r.a0;
     size_t smem = fill_smem(h->g);
-    if (h->plan.n_config > 0) {
-        const unsigned tiles = (unsigned)((int64_t)h->g.N * h->g.N);
+    if (h->plan.n_config > 0 && r.row1 > r.row0 && r.a1 >= r.a0) {
+        const unsigned tiles = (unsigned)((int64_t)(r.a1 - r.a0 + 1) * h->g.N);
         if (h->precision == BS2E_PREC_MIXED) {
             cudaFuncSetAttribute(k_csr_fill<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             k_csr_fill<true><<<tiles, 128, smem, h->stream>>>(F);

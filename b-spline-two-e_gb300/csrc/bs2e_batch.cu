@@ -1,0 +1,276 @@
+// bs2e_batch.cu -- the radial stage of many bases at once.
+//
+// A ragged batch (each basis with its own order, spline count, knot grid and
+// multipole range) runs bs2e_slater + bs2e_rk of every handle as four
+// persistent kernels (tabulation, moments, pair totals, R^k store), each
+// draining one work queue that spans all problems, so small problems do not
+// leave the GPU idle and there is one launch per stage instead of one per
+// problem and stage.  The first run tunes the R^k stage (threads per CTA,
+// items taken per queue access) by timing each candidate; the four stages are
+// then captured once in a CUDA graph and later runs replay it.  Results are
+// bit-identical to the per-handle path: both run the same device functions.
+//
+// Reference: setup_Slater_integrals and compute_R_k_map
+// (src/mat_els/mat_els.f90:172-292, src/tools/sparse_array_tools.f90:452-493),
+// which the reference runs for one basis per basis_setup invocation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "bs2e_internal.h"
+
+using namespace bs2e;
+
+struct bs2e_batch {
+    std::vector<bs2e_handle *> hs;  // in queue order (largest R^k store first)
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    RadialDev *d_probs = nullptr;
+    int64_t *d_off = nullptr;                // 4 stages x (n + 1)
+    unsigned long long *d_counter = nullptr;  // 4 counters
+    std::vector<int64_t> off[4];
+    size_t smem[4] = {0, 0, 0, 0};
+    int threads[4] = {128, 256, 256, 256};
+    int grid[4] = {1, 1, 1, 1};
+    int chunk = 1;
+    int sms = 0;
+    bool tuned = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+    std::string err;
+};
+
+namespace {
+
+constexpr int kTotThreads = 256;
+
+// Locks every handle of the batch (in address order, so two batches sharing
+// handles cannot deadlock).
+struct LockAll {
+    std::vector<std::unique_lock<std::mutex>> lk;
+    explicit LockAll(const std::vector<bs2e_handle *> &hs) {
+        std::vector<bs2e_handle *> s(hs);
+        std::sort(s.begin(), s.end());
+        for (bs2e_handle *h : s) lk.emplace_back(h->mu);
+    }
+};
+
+bs2e_status bfail(bs2e_batch *b, bs2e_status st, const std::string &m) {
+    b->err = m;
+    for (bs2e_handle *h : b->hs) h->err = m;  // readable through any handle
+    return st;
+}
+
+#define BCU(call)                                                                             \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return bfail(b, e_ == cudaErrorMemoryAllocation ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA, \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                 \
+    } while (0)
+
+// Persistent grid of a stage: every CTA the SMs hold at once (no more than
+// there are items).  Also sets the kernel's shared-memory limit, so it is
+// called outside graph capture.
+void set_grid(bs2e_batch *b, int stage) {
+    int per = radial_batch_blocks_per_sm(stage, b->threads[stage], b->smem[stage]);
+    if (per < 1) per = 1;
+    int64_t items = b->off[stage].back();
+    b->grid[stage] = (int)std::min<int64_t>((int64_t)per * b->sms, std::max<int64_t>(items, 1));
+}
+
+void enqueue_stage(bs2e_batch *b, int stage, int chunk) {
+    const int n = (int)b->hs.size();
+    launch_radial_batch(b->stream, stage, b->grid[stage], b->threads[stage], b->smem[stage],
+                        b->d_probs, b->d_off + (size_t)stage * (n + 1), n, b->d_counter + stage,
+                        stage == 3 ? chunk : 1);
+    b->launches++;
+}
+
+void enqueue_all(bs2e_batch *b) {
+    cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(unsigned long long), b->stream);
+    for (int st = 0; st < 4; ++st) enqueue_stage(b, st, b->chunk);
+}
+
+// Times the R^k stage for each candidate shape and keeps the fastest.
+bs2e_status tune(bs2e_batch *b) {
+    const int cand_threads[3] = {128, 256, 512};
+    const int cand_chunk[3] = {1, 2, 8};
+    cudaEvent_t e0, e1;
+    BCU(cudaEventCreate(&e0));
+    BCU(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bt = 256, bc = 1;
+    for (int t : cand_threads)
+        for (int c : cand_chunk) {
+            b->threads[3] = t;
+            set_grid(b, 3);
+            BCU(cudaMemsetAsync(b->d_counter + 3, 0, sizeof(unsigned long long), b->stream));
+            BCU(cudaEventRecord(e0, b->stream));
+            enqueue_stage(b, 3, c);
+            BCU(cudaEventRecord(e1, b->stream));
+            BCU(cudaEventSynchronize(e1));
+            BCU(cudaGetLastError());
+            float ms = 0.f;
+            BCU(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bt = t;
+                bc = c;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->threads[3] = bt;
+    b->chunk = bc;
+    set_grid(b, 3);
+    b->tuned = true;
+    return BS2E_OK;
+}
+
+void mark_done(bs2e_batch *b) {
+    for (bs2e_handle *h : b->hs) {
+        h->slater_done = true;
+        std::fill(h->rk_done.begin(), h->rk_done.end(), 1);
+    }
+}
+
+}  // namespace
+
+BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, bs2e_batch **out) {
+    if (!out || !handles || n < 1 || n > (1 << 20)) return BS2E_ERR_ARG;
+    *out = nullptr;
+    std::vector<bs2e_handle *> hs(handles, handles + n);
+    for (bs2e_handle *h : hs)
+        if (!h) return BS2E_ERR_ARG;
+    {
+        std::vector<bs2e_handle *> s(hs);
+        std::sort(s.begin(), s.end());
+        if (std::adjacent_find(s.begin(), s.end()) != s.end()) return BS2E_ERR_ARG;
+    }
+    const int dev = hs[0]->device;
+    for (bs2e_handle *h : hs)
+        if (h->device != dev) {
+            hs[0]->err = "batch: every handle must be on the same device";
+            return BS2E_ERR_ARG;
+        }
+    bs2e_batch *b = new (std::nothrow) bs2e_batch();
+    if (!b) return BS2E_ERR_NOMEM;
+    // largest R^k store first: the long items start early
+    std::stable_sort(hs.begin(), hs.end(), [](const bs2e_handle *x, const bs2e_handle *y) {
+        return (int64_t)x->g.N * x->g.N * x->g.tile > (int64_t)y->g.N * y->g.N * y->g.tile;
+    });
+    b->hs = hs;
+    b->device = dev;
+    bs2e_status st = BS2E_OK;
+    {
+        LockAll L(b->hs);
+        cudaSetDevice(dev);
+        auto run = [&]() -> bs2e_status {
+            cudaDeviceProp prop;
+            BCU(cudaGetDeviceProperties(&prop, dev));
+            b->sms = prop.multiProcessorCount;
+            BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+            std::vector<RadialDev> probs;
+            for (int s = 0; s < 4; ++s) b->off[s].assign(1, 0);
+            for (bs2e_handle *h : b->hs) {
+                BCU(cudaStreamSynchronize(h->stream));
+                const Radial &g = h->g;
+                if (h->precision == BS2E_PREC_MIXED) {
+                    if (!h->d_Rf) BCU(cudaMalloc(&h->d_Rf, sizeof(float2) * (size_t)g.N * g.N * g.tile));
+                    if (!h->d_Rexp) BCU(cudaMalloc(&h->d_Rexp, sizeof(int) * (size_t)g.N * g.N * g.K1));
+                    b->smem[3] = std::max(b->smem[3], (size_t)g.K1 * g.W * g.W * sizeof(double));
+                } else if (!h->d_R) {
+                    BCU(cudaMalloc(&h->d_R, sizeof(double) * (size_t)g.N * g.N * g.tile));
+                }
+                b->smem[1] = std::max(b->smem[1], moments_smem(g));
+                probs.push_back(radial_dev(h));
+                const int64_t items[4] = {g.n_iv, (int64_t)g.n_iv * g.K1,
+                                          ((int64_t)2 * g.K1 * g.N * g.W + kTotThreads - 1) / kTotThreads,
+                                          (int64_t)g.N * g.N};
+                for (int s = 0; s < 4; ++s) b->off[s].push_back(b->off[s].back() + items[s]);
+            }
+            b->threads[2] = kTotThreads;
+            const size_t nn = b->hs.size();
+            BCU(cudaMalloc(&b->d_probs, sizeof(RadialDev) * nn));
+            BCU(cudaMalloc(&b->d_off, sizeof(int64_t) * 4 * (nn + 1)));
+            BCU(cudaMalloc(&b->d_counter, 4 * sizeof(unsigned long long)));
+            BCU(cudaMemcpy(b->d_probs, probs.data(), sizeof(RadialDev) * nn, cudaMemcpyHostToDevice));
+            for (int s = 0; s < 4; ++s)
+                BCU(cudaMemcpy(b->d_off + (size_t)s * (nn + 1), b->off[s].data(),
+                               sizeof(int64_t) * (nn + 1), cudaMemcpyHostToDevice));
+            for (int s = 0; s < 4; ++s) set_grid(b, s);
+            BCU(cudaGetLastError());
+            return BS2E_OK;
+        };
+        st = run();
+    }
+    if (st != BS2E_OK) {
+        bs2e_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_batch_run(bs2e_batch *b) {
+    if (!b) return BS2E_ERR_ARG;
+    LockAll L(b->hs);
+    cudaSetDevice(b->device);
+    for (bs2e_handle *h : b->hs) BCU(cudaStreamSynchronize(h->stream));
+    if (!b->tuned) {
+        // first run: stages 0-2 eagerly, then every candidate of stage 3
+        // (each a complete R^k pass), then the graph of all four stages
+        BCU(cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(unsigned long long), b->stream));
+        for (int s = 0; s < 3; ++s) enqueue_stage(b, s, 1);
+        BCU(cudaGetLastError());
+        bs2e_status st = tune(b);
+        if (st != BS2E_OK) return st;
+        BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_all(b);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+        if (e != cudaSuccess) return bfail(b, BS2E_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        b->graph = g;
+        BCU(cudaGraphInstantiate(&b->exec, b->graph, 0));
+        BCU(cudaStreamSynchronize(b->stream));
+        mark_done(b);
+        return BS2E_OK;
+    }
+    BCU(cudaGraphLaunch(b->exec, b->stream));
+    b->launches += 4;
+    BCU(cudaStreamSynchronize(b->stream));
+    BCU(cudaGetLastError());
+    mark_done(b);
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_batch_tuning(const bs2e_batch *b, int64_t *rk_threads, int64_t *chunk,
+                                       int64_t *graph_ready, int64_t *launches) {
+    if (!b) return BS2E_ERR_ARG;
+    if (rk_threads) *rk_threads = b->threads[3];
+    if (chunk) *chunk = b->chunk;
+    if (graph_ready) *graph_ready = b->exec ? 1 : 0;
+    if (launches) *launches = b->launches;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_batch_destroy(bs2e_batch *b) {
+    if (!b) return BS2E_OK;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->d_probs) cudaFree(b->d_probs);
+    if (b->d_off) cudaFree(b->d_off);
+    if (b->d_counter) cudaFree(b->d_counter);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return BS2E_OK;
+}

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -446,6 +447,7 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
     bs2e_default_opts(&o);
     if (opts) o = *opts;
     if (o.precision != BS2E_PREC_FP64 && o.precision != BS2E_PREC_MIXED) return BS2E_ERR_ARG;
+    if (o.stage_bytes < 0) return BS2E_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BS2E_ERR_NODEV;
     if (o.device < 0 || o.device >= ndev) return BS2E_ERR_ARG;
@@ -453,6 +455,7 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
     if (!h) return BS2E_ERR_NOMEM;
     h->device = (int)o.device;
     h->precision = (int)o.precision;
+    if (o.stage_bytes > 0) h->stage_limit = std::max<int64_t>(o.stage_bytes, 4096);
     cudaSetDevice(h->device);
     Radial &g = h->g;
     g.k = (int)k;
@@ -531,6 +534,21 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_dip_stats);
         dfree(h->d_dip_cnt);
         dfree(h->d_dip_part);
+        dfree(h->d_rptrH);
+        dfree(h->d_rptrS);
+        dfree(h->d_stage[0]);
+        dfree(h->d_stage[1]);
+        if (h->copy_stream) cudaStreamSynchronize(h->copy_stream), cudaStreamDestroy(h->copy_stream);
+        for (int b = 0; b < 2; ++b) {
+            if (h->ev_filled[b]) cudaEventDestroy(h->ev_filled[b]);
+            if (h->ev_copied[b]) cudaEventDestroy(h->ev_copied[b]);
+        }
+        dfree(h->d_mv_ptr);
+        dfree(h->d_mv_idx);
+        dfree(h->d_mv_A);
+        dfree(h->d_mv_x);
+        dfree(h->d_mv_y);
+        dfree(h->d_mv_bad);
         dfree(h->d_tab_ri);
         dfree(h->d_tab_Bi);
         dfree(h->d_mom);
@@ -695,6 +713,26 @@ BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t 
     return st;
 }
 
+BS2E_API bs2e_status bs2e_rk_export(bs2e_handle *h, int64_t k, double *out, int64_t on_device) {
+    if (!h || !out) return BS2E_ERR_ARG;
+    Guard G(h);
+    const Radial &g = h->g;
+    if (k < 0 || k >= g.K1) return fail(h, BS2E_ERR_ARG, "rk_export: multipole out of range");
+    if (!h->rk_done[k]) return fail(h, BS2E_ERR_STATE, "rk_export: multipole not built by bs2e_rk");
+    const size_t n = (size_t)g.N * g.N * g.W * g.W;
+    double *d = out;
+    if (!on_device) CU(dalloc(&d, n));
+    launch_rk_slice(h, (int)k, d);
+    bs2e_status st = BS2E_OK;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && !on_device)
+        e = cudaMemcpyAsync(out, d, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) st = fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+    bs2e_status st2 = sync_check(h, "rk_export");
+    if (!on_device) cudaFree(d);
+    return st != BS2E_OK ? st : st2;
+}
+
 BS2E_API bs2e_status bs2e_rk_get(bs2e_handle *h, const int64_t key[4], double *vals) {
     return bs2e_rk_get_batch(h, 1, key, vals);
 }
@@ -799,13 +837,10 @@ BS2E_API bs2e_status bs2e_block_count(bs2e_handle *h, const bs2e_config *configs
     return bs2e_block_count_ex(h, configs, n_config, L, 0, full, nnz_H, nnz_S);
 }
 
-BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *configs,
-                                        int64_t n_config, int64_t L, int64_t spin, int64_t full,
-                                        int64_t *H_index_ptr, int64_t *H_indices, double *H_data,
-                                        int64_t *S_index_ptr, int64_t *S_indices, double *S_data,
-                                        int64_t out_on_device) {
-    if (!h || n_config < 0) return BS2E_ERR_ARG;
-    Guard G(h);
+// Checks shared by the fill entry points: every multipole built, one-body set
+// and covering the block's l values, the block counted.
+static bs2e_status fill_ready(bs2e_handle *h, const bs2e_config *configs, int64_t n_config, int64_t L,
+                       int64_t spin, int64_t full) {
     for (int kk = 0; kk < h->g.K1; ++kk)
         if (!h->rk_done[kk]) return fail(h, BS2E_ERR_STATE, "bs2e_rk has not built every multipole");
     if (!h->have_one_body)
@@ -814,55 +849,232 @@ BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *confi
     for (int c = 0; c < h->plan.n_ch; ++c)
         if (h->plan.ch_l1[c] >= h->n_l || h->plan.ch_l2[c] >= h->n_l)
             return fail(h, BS2E_ERR_ARG, "one-body matrices do not cover every l of the block");
+    return BS2E_OK;
+}
+
+// The n_a (= n1) range of rows [r0, r1).
+static void row_tiles(const bs2e_config *cf, int64_t r0, int64_t r1, FillRange &r) {
+    int64_t a0 = INT64_MAX, a1 = 0;
+    for (int64_t i = r0; i < r1; ++i) {
+        a0 = std::min<int64_t>(a0, cf[i].n1);
+        a1 = std::max<int64_t>(a1, cf[i].n1);
+    }
+    r.a0 = (int)std::max<int64_t>(a0 == INT64_MAX ? 1 : a0, 1);
+    r.a1 = (int)a1;
+}
+
+// Range CSR pointers of rows [r0, r0 + n) into the handle's buffers.
+static bs2e_status range_ptrs(bs2e_handle *h, int64_t r0, int64_t n) {
+    if (n + 1 > h->rptr_cap) {
+        dfree(h->d_rptrH);
+        dfree(h->d_rptrS);
+        h->rptr_cap = 0;
+        CU(dalloc(&h->d_rptrH, (size_t)n + 1));
+        CU(dalloc(&h->d_rptrS, (size_t)n + 1));
+        h->rptr_cap = n + 1;
+    }
+    launch_block_scan(h, h->d_rptrH, h->d_rptrS, r0, n);
+    return BS2E_OK;
+}
+
+// Fills rows [r0, r0 + n) of the counted block into HOST arrays (range-local
+// 1-based index_ptr): the range is cut into chunks that fit one of two
+// staging areas in HBM; the fill of chunk c runs on the handle's stream while
+// the copy stream moves chunk c - 1 to the host, so the device-to-host copy
+// overlaps the assembly and device memory stays bounded.
+static bs2e_status stream_fill(bs2e_handle *h, const bs2e_config *cf, int64_t r0, int64_t n,
+                        int64_t *Hp, int64_t *Hi, double *Hd, int64_t *Sp, int64_t *Si,
+                        double *Sd) {
+    TRY(range_ptrs(h, r0, n));
+    CU(cudaMemcpyAsync(Hp, h->d_rptrH, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(Sp, h->d_rptrS, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaStreamSynchronize(h->stream));
+    const int64_t nH = Hp[n] - 1, nS = Sp[n] - 1;
+    if (nH == 0 && nS == 0) return sync_check(h, "block fill");
+    if (!h->copy_stream) {
+        CU(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            CU(cudaEventCreateWithFlags(&h->ev_filled[b], cudaEventDisableTiming));
+            CU(cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming));
+        }
+    }
+    // staging areas: the whole range if it fits, else the handle's limit
+    // (2 GiB by default; a row holds at most 2 W^2 entries per column channel)
+    const int64_t total = 24 * (nH + nS) + 64;
+    const int64_t want = std::min<int64_t>(
+        std::max<int64_t>(total, std::min<int64_t>((int64_t)64 << 20, h->stage_limit)),
+        h->stage_limit);
+    if (want > h->stage_cap) {
+        CU(cudaStreamSynchronize(h->copy_stream));
+        dfree(h->d_stage[0]);
+        dfree(h->d_stage[1]);
+        h->stage_cap = 0;
+        CU(dalloc(&h->d_stage[0], (size_t)want));
+        CU(dalloc(&h->d_stage[1], (size_t)want));
+        h->stage_cap = want;
+    }
+    const int64_t cap = h->stage_cap - 64;
+    // chunk boundaries: the most rows whose H + S entries fit one area
+    std::vector<int64_t> cut{0};
+    while (cut.back() < n) {
+        const int64_t c0 = cut.back();
+        if (24 * ((Hp[c0 + 1] - Hp[c0]) + (Sp[c0 + 1] - Sp[c0])) + 32 > cap)
+            return fail(h, BS2E_ERR_NOMEM, "block fill: one row exceeds the staging area");
+        int64_t c1 = c0 + 1, lo = c0 + 1, hi = n;
+        while (lo <= hi) {
+            int64_t mid = lo + (hi - lo) / 2;
+            if (24 * ((Hp[mid] - Hp[c0]) + (Sp[mid] - Sp[c0])) + 32 <= cap) {
+                c1 = mid;
+                lo = mid + 1;
+            } else {
+                hi = mid - 1;
+            }
+        }
+        cut.push_back(c1);
+    }
+    const int n_chunk = (int)cut.size() - 1;
+    struct Lay {
+        size_t oHd, oSi, oSd;
+        int64_t hC, sC;
+    };
+    auto lay = [&](int c) {
+        Lay L;
+        L.hC = Hp[cut[c + 1]] - Hp[cut[c]];
+        L.sC = Sp[cut[c + 1]] - Sp[cut[c]];
+        L.oHd = (size_t)((8 * L.hC + 15) / 16 * 16);
+        L.oSi = L.oHd + 16 * (size_t)L.hC;
+        L.oSd = L.oSi + (size_t)((8 * L.sC + 15) / 16 * 16);
+        return L;
+    };
+    cudaError_t e = cudaSuccess;
+    // fill of chunk c into area c % 2, after the copies out of that area (chunk
+    // c - 2) are done
+    auto fill = [&](int c) {
+        const int b = c & 1;
+        const Lay L = lay(c);
+        unsigned char *base = h->d_stage[b];
+        if (e == cudaSuccess && c >= 2) e = cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0);
+        FillRange r;
+        r.row0 = r0 + cut[c];
+        r.row1 = r0 + cut[c + 1];
+        r.ptr_row0 = r0;
+        r.Hbase = Hp[cut[c]] - 1;
+        r.Sbase = Sp[cut[c]] - 1;
+        row_tiles(cf, r.row0, r.row1, r);
+        if (e == cudaSuccess) {
+            launch_block_fill(h, r, h->d_rptrH, h->d_rptrS, (int64_t *)base,
+                              (double2 *)(base + L.oHd), (int64_t *)(base + L.oSi),
+                              (double2 *)(base + L.oSd));
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(h->ev_filled[b], h->stream);
+    };
+    auto cp = [&](void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes)
+            e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->copy_stream);
+    };
+    // the fill of chunk c + 1 is queued before the copies of chunk c are
+    // issued: a copy to pageable memory may block the host until it is done
+    fill(0);
+    for (int c = 0; c < n_chunk && e == cudaSuccess; ++c) {
+        if (c + 1 < n_chunk) fill(c + 1);
+        const int b = c & 1;
+        const Lay L = lay(c);
+        const unsigned char *base = h->d_stage[b];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->copy_stream, h->ev_filled[b], 0);
+        cp(Hi + (Hp[cut[c]] - 1), base, 8 * (size_t)L.hC);
+        cp(Hd + 2 * (Hp[cut[c]] - 1), base + L.oHd, 16 * (size_t)L.hC);
+        cp(Si + (Sp[cut[c]] - 1), base + L.oSi, 8 * (size_t)L.sC);
+        cp(Sd + 2 * (Sp[cut[c]] - 1), base + L.oSd, 16 * (size_t)L.sC);
+        if (e == cudaSuccess) e = cudaEventRecord(h->ev_copied[b], h->copy_stream);
+    }
+    cudaError_t e2 = cudaStreamSynchronize(h->copy_stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(h->stream);
+        return fail(h, e == cudaErrorMemoryAllocation ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA,
+                    std::string("block fill (streamed): ") + cudaGetErrorString(e));
+    }
+    return sync_check(h, "block fill");
+}
+
+BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *configs,
+                                        int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                        int64_t *H_index_ptr, int64_t *H_indices, double *H_data,
+                                        int64_t *S_index_ptr, int64_t *S_indices, double *S_data,
+                                        int64_t out_on_device) {
+    if (!h || n_config < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    TRY(fill_ready(h, configs, n_config, L, spin, full));
     const int64_t nH = h->blk.nnzH, nS = h->blk.nnzS;
     if (!H_index_ptr || !S_index_ptr || (nH > 0 && (!H_indices || !H_data)) ||
         (nS > 0 && (!S_indices || !S_data)))
         return fail(h, BS2E_ERR_ARG, "NULL output array");
-    int64_t *dHp, *dSp, *dHi, *dSi;
-    double2 *dHd, *dSd;
-    bool dev = out_on_device != 0;
-    if (dev) {
-        dHp = H_index_ptr;
-        dSp = S_index_ptr;
-        dHi = H_indices;
-        dSi = S_indices;
-        dHd = (double2 *)H_data;
-        dSd = (double2 *)S_data;
-    } else {
-        CU(dalloc(&dHp, (size_t)n_config + 1));
-        CU(dalloc(&dSp, (size_t)n_config + 1));
-        CU(dalloc(&dHi, (size_t)nH));
-        CU(dalloc(&dSi, (size_t)nS));
-        CU(dalloc(&dHd, (size_t)nH));
-        CU(dalloc(&dSd, (size_t)nS));
-    }
-    launch_block_scan(h, dHp, dSp);
-    launch_block_fill(h, dHp, dSp, dHi, dHd, dSi, dSd);
-    bs2e_status st = BS2E_OK;
-    if (!dev) {
-        cudaError_t e = cudaSuccess;
-        auto cp = [&](void *dst, const void *src, size_t bytes) {
-            if (e == cudaSuccess && bytes)
-                e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
-        };
-        cp(H_index_ptr, dHp, sizeof(int64_t) * (n_config + 1));
-        cp(S_index_ptr, dSp, sizeof(int64_t) * (n_config + 1));
-        cp(H_indices, dHi, sizeof(int64_t) * nH);
-        cp(H_data, dHd, sizeof(double2) * nH);
-        cp(S_indices, dSi, sizeof(int64_t) * nS);
-        cp(S_data, dSd, sizeof(double2) * nS);
-        if (e != cudaSuccess) st = fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
-    }
-    bs2e_status st2 = sync_check(h, "block fill");
-    if (!dev) {
-        cudaFree(dHp);
-        cudaFree(dSp);
-        cudaFree(dHi);
-        cudaFree(dSi);
-        cudaFree(dHd);
-        cudaFree(dSd);
-    }
-    return st != BS2E_OK ? st : st2;
+    if (!out_on_device)
+        return stream_fill(h, configs, 0, n_config, H_index_ptr, H_indices, H_data, S_index_ptr,
+                           S_indices, S_data);
+    launch_block_scan(h, H_index_ptr, S_index_ptr, 0, n_config);
+    FillRange r;
+    r.row0 = 0;
+    r.row1 = n_config;
+    r.a0 = 1;
+    r.a1 = h->g.N;
+    launch_block_fill(h, r, H_index_ptr, S_index_ptr, H_indices, (double2 *)H_data, S_indices,
+                      (double2 *)S_data);
+    CU(cudaGetLastError());
+    return sync_check(h, "block fill");
+}
+
+// Rows [row_first, row_first + row_count) of a block.
+static bs2e_status check_rows(bs2e_handle *h, int64_t n_config, int64_t row_first, int64_t row_count) {
+    if (row_first < 0 || row_count < 0 || row_first + row_count > n_config)
+        return fail(h, BS2E_ERR_ARG, "row range outside the block");
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_block_count_rows(bs2e_handle *h, const bs2e_config *configs,
+                                           int64_t n_config, int64_t L, int64_t spin,
+                                           int64_t full, int64_t row_first, int64_t row_count,
+                                           int64_t *nnz_H, int64_t *nnz_S) {
+    if (!h || n_config < 0 || !nnz_H || !nnz_S) return BS2E_ERR_ARG;
+    Guard G(h);
+    TRY(check_rows(h, n_config, row_first, row_count));
+    TRY(ensure_counted(h, configs, n_config, L, spin, full));
+    TRY(range_ptrs(h, row_first, row_count));
+    int64_t eH = 1, eS = 1;
+    CU(cudaMemcpyAsync(&eH, h->d_rptrH + row_count, 8, cudaMemcpyDeviceToHost, h->stream));
+    CU(cudaMemcpyAsync(&eS, h->d_rptrS + row_count, 8, cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "block count (rows)"));
+    *nnz_H = eH - 1;
+    *nnz_S = eS - 1;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *configs,
+                                          int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                          int64_t row_first, int64_t row_count,
+                                          int64_t *H_index_ptr, int64_t *H_indices,
+                                          double *H_data, int64_t *S_index_ptr,
+                                          int64_t *S_indices, double *S_data,
+                                          int64_t out_on_device) {
+    if (!h || n_config < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    TRY(check_rows(h, n_config, row_first, row_count));
+    TRY(fill_ready(h, configs, n_config, L, spin, full));
+    if (!H_index_ptr || !S_index_ptr) return fail(h, BS2E_ERR_ARG, "NULL output array");
+    if (!out_on_device)
+        return stream_fill(h, configs, row_first, row_count, H_index_ptr, H_indices, H_data,
+                           S_index_ptr, S_indices, S_data);
+    launch_block_scan(h, H_index_ptr, S_index_ptr, row_first, row_count);
+    FillRange r;
+    r.row0 = row_first;
+    r.row1 = row_first + row_count;
+    r.ptr_row0 = row_first;
+    row_tiles(configs, r.row0, r.row1, r);
+    launch_block_fill(h, r, H_index_ptr, S_index_ptr, H_indices, (double2 *)H_data, S_indices,
+                      (double2 *)S_data);
+    CU(cudaGetLastError());
+    return sync_check(h, "block fill (rows)");
 }
 
 BS2E_API bs2e_status bs2e_block_fill(bs2e_handle *h, const bs2e_config *configs,
@@ -1026,3 +1238,228 @@ BS2E_API bs2e_status bs2e_synchronize(bs2e_handle *h) {
 }
 
 }  // extern "C"
+
+// CSR_mv / CSR_T_mv / CSR_mv_sym (sparse_array_tools.f90:966-1074).
+BS2E_API bs2e_status bs2e_csr_mv(bs2e_handle *h, int64_t op, int64_t n_rows, int64_t n_cols,
+                                 int64_t nnz, const int64_t *index_ptr, const int64_t *indices,
+                                 const double *data, const double *x, double *y,
+                                 int64_t on_device) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard g(h);
+    if (op < 0 || op > 2) return fail(h, BS2E_ERR_ARG, "csr_mv: op must be 0 (N), 1 (T) or 2 (sym)");
+    if (n_rows < 0 || n_cols < 0 || nnz < 0 || n_rows > ((int64_t)1 << 34))
+        return fail(h, BS2E_ERR_ARG, "csr_mv: negative or too large sizes");
+    if (op == 2 && n_rows != n_cols)
+        return fail(h, BS2E_ERR_ARG, "csr_mv: the symmetric product needs a square matrix");
+    const int64_t n_out = op == 1 ? n_cols : n_rows, n_in = op == 1 ? n_rows : n_cols;
+    if (!index_ptr || !x || !y || (nnz > 0 && (!indices || !data)))
+        return fail(h, BS2E_ERR_ARG, "csr_mv: NULL array");
+    if (!h->d_mv_bad) CU(dalloc(&h->d_mv_bad, 1));
+    CU(cudaMemsetAsync(h->d_mv_bad, 0, sizeof(int), h->stream));
+    const int64_t *dp = index_ptr, *di = indices;
+    const double2 *dA = (const double2 *)data, *dx = (const double2 *)x;
+    double2 *dy = (double2 *)y;
+    if (!on_device) {
+        if (index_ptr[n_rows] - 1 != nnz)
+            return fail(h, BS2E_ERR_ARG, "csr_mv: index_ptr(n_rows+1) - 1 differs from nnz");
+        CU(grow(&h->d_mv_ptr, h->mv_ptr_cap, n_rows + 1));
+        CU(grow(&h->d_mv_idx, h->mv_idx_cap, nnz));
+        CU(grow(&h->d_mv_A, h->mv_A_cap, nnz));
+        CU(grow(&h->d_mv_x, h->mv_x_cap, n_in));
+        CU(grow(&h->d_mv_y, h->mv_y_cap, n_out));
+        CU(cudaMemcpyAsync(h->d_mv_ptr, index_ptr, 8 * (size_t)(n_rows + 1),
+                           cudaMemcpyHostToDevice, h->stream));
+        if (nnz > 0) {
+            CU(cudaMemcpyAsync(h->d_mv_idx, indices, 8 * (size_t)nnz, cudaMemcpyHostToDevice,
+                               h->stream));
+            CU(cudaMemcpyAsync(h->d_mv_A, data, 16 * (size_t)nnz, cudaMemcpyHostToDevice,
+                               h->stream));
+        }
+        if (n_in > 0)
+            CU(cudaMemcpyAsync(h->d_mv_x, x, 16 * (size_t)n_in, cudaMemcpyHostToDevice,
+                               h->stream));
+        dp = h->d_mv_ptr;
+        di = h->d_mv_idx;
+        dA = h->d_mv_A;
+        dx = h->d_mv_x;
+        dy = h->d_mv_y;
+    }
+    launch_csr_mv(h, (int)op, n_rows, n_cols, nnz, dp, di, dA, dx, dy, h->d_mv_bad);
+    CU(cudaGetLastError());
+    if (!on_device && n_out > 0)
+        CU(cudaMemcpyAsync(y, dy, 16 * (size_t)n_out, cudaMemcpyDeviceToHost, h->stream));
+    int bad = 0;
+    CU(cudaMemcpyAsync(&bad, h->d_mv_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync_check(h, "csr_mv"));
+    if (bad & 1) return fail(h, BS2E_ERR_ARG, "csr_mv: index_ptr out of range or decreasing");
+    if (bad & 2) return fail(h, BS2E_ERR_ARG, "csr_mv: column index outside 1..n_cols");
+    return BS2E_OK;
+}
+
+// CS_from_block / CSR_from_block (block_tools.f90:153-234).
+BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t n_cb,
+                                          const int64_t *shapes, const int64_t *nnz,
+                                          const int64_t *const *index_ptr,
+                                          const int64_t *const *indices,
+                                          const double *const *data, int64_t *out_index_ptr,
+                                          int64_t *out_indices, double *out_data,
+                                          int64_t on_device) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard g(h);
+    if (n_rb < 1 || n_cb < 1 || n_rb * n_cb > (1 << 20) || !shapes || !nnz || !out_index_ptr)
+        return fail(h, BS2E_ERR_ARG, "csr_from_blocks: bad block grid or NULL array");
+    const int64_t nb = n_rb * n_cb;
+    std::vector<int64_t> row0(n_rb + 1, 0);
+    int64_t tot = 0;
+    for (int64_t i = 0; i < n_rb; ++i) {
+        const int64_t rows = shapes[2 * i];  // block (i, 1) gives the row count
+        if (rows < 0) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: negative shape");
+        for (int64_t j = 0; j < n_cb; ++j) {
+            const int64_t b = i + n_rb * j;
+            if (shapes[2 * b] < 0 || shapes[2 * b + 1] < 0 || nnz[b] < 0)
+                return fail(h, BS2E_ERR_ARG, "csr_from_blocks: negative shape or nnz");
+            if (nnz[b] > 0 && shapes[2 * b] != rows)
+                return fail(h, BS2E_ERR_ARG, "csr_from_blocks: blocks of one block row differ in rows");
+            if (nnz[b] > 0 && (!index_ptr || !indices || !data || !index_ptr[b] || !indices[b] || !data[b]))
+                return fail(h, BS2E_ERR_ARG, "csr_from_blocks: NULL array of a non-empty block");
+            tot += nnz[b];
+        }
+        row0[i + 1] = row0[i] + rows;
+    }
+    const int64_t n_rows = row0[n_rb];
+    if (tot > 0 && (!out_indices || !out_data)) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: NULL output");
+    if (n_rows == 0) {
+        if (tot > 0) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: entries in blocks without rows");
+        const int64_t one = 1;
+        if (!on_device) {
+            out_index_ptr[0] = 1;
+            return BS2E_OK;
+        }
+        CU(cudaMemcpy(out_index_ptr, &one, 8, cudaMemcpyHostToDevice));
+        return BS2E_OK;
+    }
+    std::vector<CatBlock> cb(nb);
+    // host operands are staged: one device area for every non-empty block
+    std::vector<void *> staged;
+    auto cleanup = [&]() {
+        for (void *p : staged) cudaFree(p);
+    };
+    for (int64_t i = 0; i < n_rb; ++i) {
+        int64_t col = 0;
+        for (int64_t j = 0; j < n_cb; ++j) {
+            const int64_t b = i + n_rb * j;
+            CatBlock &B = cb[b];
+            B.nnz = nnz[b];
+            B.n_cols = shapes[2 * b + 1];
+            B.col0 = col;
+            B.ptr = nullptr;
+            B.idx = nullptr;
+            B.data = nullptr;
+            col += shapes[2 * b + 1];
+            if (nnz[b] <= 0) continue;
+            if (on_device) {
+                B.ptr = index_ptr[b];
+                B.idx = indices[b];
+                B.data = (const double2 *)data[b];
+                continue;
+            }
+            const int64_t rows = shapes[2 * b];
+            char *d = nullptr;
+            const size_t bytes = 8 * (size_t)(rows + 1) + 8 * (size_t)nnz[b] + 16 * (size_t)nnz[b];
+            cudaError_t e = cudaMalloc(&d, bytes);
+            if (e != cudaSuccess) {
+                cleanup();
+                return fail(h, BS2E_ERR_NOMEM, "csr_from_blocks: staging");
+            }
+            staged.push_back(d);
+            int64_t *dp = (int64_t *)d, *di = dp + rows + 1;
+            double2 *dd = (double2 *)(di + nnz[b]);
+            e = cudaMemcpyAsync(dp, index_ptr[b], 8 * (size_t)(rows + 1), cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(di, indices[b], 8 * (size_t)nnz[b], cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(dd, data[b], 16 * (size_t)nnz[b], cudaMemcpyHostToDevice, h->stream);
+            if (e != cudaSuccess) {
+                cudaStreamSynchronize(h->stream);
+                cleanup();
+                return fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+            }
+            B.ptr = dp;
+            B.idx = di;
+            B.data = dd;
+        }
+    }
+    // device tables, counts, scan partials, flag, and (host mode) outputs
+    const size_t nparts = (size_t)(n_rows + 4095) / 4096 + 4;
+    size_t tbytes = sizeof(CatBlock) * nb + 8 * (size_t)(n_rb + 1) + 8 * (size_t)(n_rows + 1) +
+                    8 * nparts + 16;
+    size_t obytes = on_device ? 0 : 8 * (size_t)(n_rows + 1) + 24 * (size_t)tot + 16;
+    char *t = nullptr;
+    cudaError_t e = cudaMalloc(&t, tbytes + obytes);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(h, BS2E_ERR_NOMEM, "csr_from_blocks: work area");
+    }
+    staged.push_back(t);
+    CatBlock *d_cb = (CatBlock *)t;
+    int64_t *d_row0 = (int64_t *)(t + sizeof(CatBlock) * nb);
+    int64_t *d_cnt = d_row0 + n_rb + 1;
+    int64_t *d_part = d_cnt + n_rows + 1;
+    int *d_bad = (int *)(d_part + nparts);
+    int64_t *optr = out_index_ptr, *oidx = out_indices;
+    double2 *odat = (double2 *)out_data;
+    if (!on_device) {
+        char *o = t + tbytes;
+        optr = (int64_t *)o;
+        oidx = optr + n_rows + 1;
+        odat = (double2 *)(((uintptr_t)(oidx + tot) + 15) & ~(uintptr_t)15);
+    }
+    e = cudaMemcpyAsync(d_cb, cb.data(), sizeof(CatBlock) * nb, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_row0, row0.data(), 8 * (size_t)(n_rb + 1), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0, sizeof(int), h->stream);
+    CatArgs A;
+    A.blocks = d_cb;
+    A.row0 = d_row0;
+    A.n_rb = (int)n_rb;
+    A.n_cb = (int)n_cb;
+    A.n_rows = n_rows;
+    if (e == cudaSuccess) {
+        launch_cat(h, A, d_cnt, d_part, optr, nullptr, nullptr, d_bad, false);
+        e = cudaGetLastError();
+    }
+    int64_t last = 1;
+    int bad = 0;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&last, optr + n_rows, 8, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (bad || last - 1 != tot) {
+        cleanup();
+        return fail(h, BS2E_ERR_ARG, "csr_from_blocks: a block index_ptr is out of range or "
+                                     "disagrees with its nnz");
+    }
+    if (tot > 0) {
+        launch_cat(h, A, nullptr, nullptr, optr, oidx, odat, d_bad, true);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && !on_device) {
+        e = cudaMemcpyAsync(out_index_ptr, optr, 8 * (size_t)(n_rows + 1), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess && tot > 0)
+            e = cudaMemcpyAsync(out_indices, oidx, 8 * (size_t)tot, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess && tot > 0)
+            e = cudaMemcpyAsync(out_data, odat, 16 * (size_t)tot, cudaMemcpyDeviceToHost, h->stream);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cleanup();
+    if (e != cudaSuccess) return fail(h, BS2E_ERR_CUDA, cudaGetErrorString(e));
+    if (bad & 2) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: a column index exceeds its block's width");
+    return BS2E_OK;
+}

@@ -153,6 +153,20 @@ struct bs2e_handle {
     unsigned long long *d_dip_stats = nullptr;
     int64_t *d_dip_cnt = nullptr, *d_dip_part = nullptr;
     int64_t dip_cnt_cap = 0, dip_part_cap = 0;
+    // host-output fills: range CSR pointers, two staging areas in HBM and the
+    // stream that copies a filled area to the host while the next one fills
+    int64_t *d_rptrH = nullptr, *d_rptrS = nullptr;
+    int64_t rptr_cap = 0;
+    unsigned char *d_stage[2] = {nullptr, nullptr};
+    int64_t stage_cap = 0;
+    int64_t stage_limit = (int64_t)2 << 30;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_filled[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+    // mat-vec staging for host operands, and its bad-input flag word
+    int64_t *d_mv_ptr = nullptr, *d_mv_idx = nullptr;
+    double2 *d_mv_A = nullptr, *d_mv_x = nullptr, *d_mv_y = nullptr;
+    int64_t mv_ptr_cap = 0, mv_idx_cap = 0, mv_A_cap = 0, mv_x_cap = 0, mv_y_cap = 0;
+    int *d_mv_bad = nullptr;
 };
 
 namespace bs2e {
@@ -166,14 +180,53 @@ void gauss_legendre(int q, double *x, double *w);
 void plan_channels(BlockPlan &plan, int K1);
 
 // Kernel launchers (bs2e_radial.cu)
+// Device view of one handle's radial buffers (the single-handle kernels and
+// the batched ones read the same struct).
+struct RadialDev {
+    const double *knots, *glx, *glw;
+    double *tab_r, *tab_B, *tab_D2, *tab_D1, *tab_ri, *tab_Bi;
+    double *mom, *dint, *tot, *R;
+    float2 *Rf;
+    int *Rexp;
+    int k, q, K1, N, n_iv, mixed;
+    int64_t tile;
+};
+RadialDev radial_dev(const bs2e_handle *h);
+// batched radial stages (0 tabulate, 1 moments, 2 totals, 3 R^k store)
+int radial_batch_blocks_per_sm(int stage, int threads, size_t smem);
+void launch_radial_batch(cudaStream_t s, int stage, int grid, int threads, size_t smem,
+                         const RadialDev *probs, const int64_t *off, int n,
+                         unsigned long long *counter, int chunk);
+size_t moments_smem(const Radial &g);
 void launch_tabulate(bs2e_handle *h);
 void launch_moments(bs2e_handle *h);
 void launch_totals(bs2e_handle *h);
 void launch_rk_fill(bs2e_handle *h, int k_first, int k_count);
 void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *d_vals);
+void launch_rk_slice(bs2e_handle *h, int kk, double *d_out);
 void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, double cap_r0,
                      double eta_re, double eta_im);
 void launch_band_split(bs2e_handle *h);
+// One block of a block matrix being joined into one CSR (device pointers).
+struct CatBlock {
+    const int64_t *ptr, *idx;
+    const double2 *data;
+    int64_t nnz, n_cols, col0;
+};
+struct CatArgs {
+    const CatBlock *blocks;  // [n_rb * n_cb], block (i, j) at i + n_rb * j
+    const int64_t *row0;     // [n_rb + 1] first output row of each block row
+    int n_rb, n_cb;
+    int64_t n_rows;
+};
+// copy = false: row lengths into cnt and the 1-based index_ptr into optr;
+// copy = true: the entries into oidx / odat
+void launch_cat(bs2e_handle *h, const CatArgs &A, int64_t *cnt, int64_t *part, int64_t *optr,
+                int64_t *oidx, double2 *odat, int *bad, bool copy);
+void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr);
+void launch_csr_mv(bs2e_handle *h, int op, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                   const int64_t *ptr, const int64_t *idx, const double2 *A, const double2 *x,
+                   double2 *y, int *bad);
 // Kernel launchers (bs2e_dipole.cu)
 void launch_radial_dip(bs2e_handle *h, int gauge);
 void launch_dip_count(bs2e_handle *h, const DipDev &D, int64_t *cnt);
@@ -189,8 +242,17 @@ void launch_chan_marks_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, int
 void launch_plan_seg_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, const int *lmap,
                         int segS, int *base, int *lo, int *hi, unsigned long long *stats);
 void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr);
-void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr);
-void launch_block_fill(bs2e_handle *h, const int64_t *d_Hptr, const int64_t *d_Sptr,
-                       int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx, double2 *d_Sdat);
+// Rows [row0, row1) of the counted block; their tiles have n_a in [a0, a1].
+// Row r's entries start at output position ptr[r - ptr_row0] - 1 - base.
+struct FillRange {
+    int64_t row0 = 0, row1 = 0, ptr_row0 = 0, Hbase = 0, Sbase = 0;
+    int a0 = 1, a1 = 0;
+};
+// 1-based CSR pointers of rows [row0, row0 + n) (n + 1 entries, starting at 1)
+void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr, int64_t row0,
+                       int64_t n);
+void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr,
+                       const int64_t *d_Sptr, int64_t *d_Hidx, double2 *d_Hdat, int64_t *d_Sidx,
+                       double2 *d_Sdat);
 
 }  // namespace bs2e

@@ -71,34 +71,35 @@ __device__ __forceinline__ double powi(double x, int n) {
 // ---------------------------------------------------------------------------
 // K1: tabulation.  One CTA per breakpoint interval.
 // ---------------------------------------------------------------------------
-__global__ void k_tabulate(const double *__restrict__ knots, const double *__restrict__ glx,
-                           int k, int q, double *__restrict__ tab_r, double *__restrict__ tab_B,
-                           double *__restrict__ tab_D2, double *__restrict__ tab_D1,
-                           double *__restrict__ tab_ri, double *__restrict__ tab_Bi) {
-    const int iv = blockIdx.x;
+__device__ void tabulate_iv(const RadialDev &P, int iv) {
+    const int k = P.k, q = P.q;
+    const double *__restrict__ knots = P.knots;
+    const double *__restrict__ glx = P.glx;
     const int iv1 = iv + 1;
     const double lo = knots[k - 1 + iv], hi = knots[k + iv];
     const double sc = __dmul_rn(0.5, __dsub_rn(hi, lo));
     const double tr = __dmul_rn(0.5, __dadd_rn(hi, lo));
     for (int e = threadIdx.x; e < q * k; e += blockDim.x) {
-        int P = e / k, s = e - P * k;
-        double r = __dadd_rn(__dmul_rn(sc, glx[P]), tr);
-        if (s == 0) tab_r[(size_t)iv * q + P] = r;
-        tab_B[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 0, iv1, iv1 + s);
-        tab_D2[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 2, iv1, iv1 + s);
-        tab_D1[((size_t)iv * q + P) * k + s] = bval(knots, k, r, 1, iv1, iv1 + s);
+        int Pp = e / k, s = e - Pp * k;
+        double r = __dadd_rn(__dmul_rn(sc, glx[Pp]), tr);
+        if (s == 0) P.tab_r[(size_t)iv * q + Pp] = r;
+        P.tab_B[((size_t)iv * q + Pp) * k + s] = bval(knots, k, r, 0, iv1, iv1 + s);
+        P.tab_D2[((size_t)iv * q + Pp) * k + s] = bval(knots, k, r, 2, iv1, iv1 + s);
+        P.tab_D1[((size_t)iv * q + Pp) * k + s] = bval(knots, k, r, 1, iv1, iv1 + s);
     }
     for (int e = threadIdx.x; e < q * q * k; e += blockDim.x) {
-        int s = e % k, PQ = e / k, Q = PQ % q, P = PQ / q;
-        double r = __dadd_rn(__dmul_rn(sc, glx[P]), tr);
+        int s = e % k, PQ = e / k, Q = PQ % q, Pp = PQ / q;
+        double r = __dadd_rn(__dmul_rn(sc, glx[Pp]), tr);
         double scj = __dmul_rn(0.5, __dsub_rn(r, lo));
         double trj = __dmul_rn(0.5, __dadd_rn(r, lo));
         double rj = __dadd_rn(__dmul_rn(scj, glx[Q]), trj);
-        size_t o = ((size_t)iv * q + P) * q + Q;
-        if (s == 0) tab_ri[o] = rj;
-        tab_Bi[o * k + s] = bval(knots, k, rj, 0, iv1, iv1 + s);
+        size_t o = ((size_t)iv * q + Pp) * q + Q;
+        if (s == 0) P.tab_ri[o] = rj;
+        P.tab_Bi[o * k + s] = bval(knots, k, rj, 0, iv1, iv1 + s);
     }
 }
+
+__global__ void k_tabulate(RadialDev P) { tabulate_iv(P, blockIdx.x); }
 
 // ---------------------------------------------------------------------------
 // K2: moments and same-interval integrals.  One CTA per (interval, multipole).
@@ -108,13 +109,16 @@ __global__ void k_tabulate(const double *__restrict__ knots, const double *__res
 //   J_q(P) = h_P sum_Q w_Q B_j(rho_PQ) B_j'(rho_PQ) rho_PQ^kk  on [t_iv, r_P]
 // (compute_Slater_off_diag / compute_Slater_diag, mat_els.f90:392-491).
 // ---------------------------------------------------------------------------
-__global__ void k_moments(const double *__restrict__ knots, const double *__restrict__ glw, int k,
-                          int q, int K1, const double *__restrict__ tab_r,
-                          const double *__restrict__ tab_B, const double *__restrict__ tab_ri,
-                          const double *__restrict__ tab_Bi, double *__restrict__ mom,
-                          double *__restrict__ dint) {
-    extern __shared__ double sm[];
-    const int iv = blockIdx.x, kk = blockIdx.y;
+__device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
+    const int k = Pd.k, q = Pd.q, K1 = Pd.K1;
+    const double *__restrict__ knots = Pd.knots;
+    const double *__restrict__ glw = Pd.glw;
+    const double *__restrict__ tab_r = Pd.tab_r;
+    const double *__restrict__ tab_B = Pd.tab_B;
+    const double *__restrict__ tab_ri = Pd.tab_ri;
+    const double *__restrict__ tab_Bi = Pd.tab_Bi;
+    double *__restrict__ mom = Pd.mom;
+    double *__restrict__ dint = Pd.dint;
     const int kq = k * q, k2 = k * k;
     double *sB = sm;              // [q][k]
     double *sR = sB + kq;         // [q]
@@ -176,32 +180,43 @@ __global__ void k_moments(const double *__restrict__ knots, const double *__rest
     }
 }
 
+__global__ void k_moments(RadialDev P) {
+    extern __shared__ double sm[];
+    moments_item(P, blockIdx.x, blockIdx.y, sm);
+}
+
 // ---------------------------------------------------------------------------
 // K3: pair totals tot[which][kk][a][dc] = sum over shared intervals of mom.
 // ---------------------------------------------------------------------------
-__global__ void k_totals(const double *__restrict__ mom, int k, int K1, int N, int n_iv,
-                         double *__restrict__ tot) {
-    const int W = 2 * k - 1;
-    const int64_t total = (int64_t)2 * K1 * N * W;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-         e += (int64_t)gridDim.x * blockDim.x) {
-        int dc = (int)(e % W);
-        int64_t r = e / W;
-        int a = (int)(r % N);
-        r /= N;
-        int kk = (int)(r % K1);
-        int which = (int)(r / K1);
-        int c = a + dc - (k - 1);
-        double s = 0.0;
-        if (c >= 0 && c < N) {
-            int lo = max(max(a, c) - k + 2, 0), hi = min(min(a, c) + 1, n_iv - 1);
-            for (int iv = lo; iv <= hi; ++iv) {
-                int sa = a + 1 - iv, scc = c + 1 - iv;
-                s += mom[(((size_t)iv * K1 + kk) * 2 + which) * k * k + sa * k + scc];
-            }
+__device__ __forceinline__ void totals_elem(const RadialDev &P, int64_t e) {
+    const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1;
+    int dc = (int)(e % W);
+    int64_t r = e / W;
+    int a = (int)(r % N);
+    r /= N;
+    int kk = (int)(r % K1);
+    int which = (int)(r / K1);
+    int c = a + dc - (k - 1);
+    double s = 0.0;
+    if (c >= 0 && c < N) {
+        int lo = max(max(a, c) - k + 2, 0), hi = min(min(a, c) + 1, n_iv - 1);
+        for (int iv = lo; iv <= hi; ++iv) {
+            int sa = a + 1 - iv, scc = c + 1 - iv;
+            s += P.mom[(((size_t)iv * K1 + kk) * 2 + which) * k * k + sa * k + scc];
         }
-        tot[e] = s;
     }
+    P.tot[e] = s;
+}
+
+__device__ __forceinline__ int64_t totals_count(const RadialDev &P) {
+    return (int64_t)2 * P.K1 * P.N * (2 * P.k - 1);
+}
+
+__global__ void k_totals(RadialDev P) {
+    const int64_t total = totals_count(P);
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x)
+        totals_elem(P, e);
 }
 
 // ---------------------------------------------------------------------------
@@ -252,14 +267,13 @@ __device__ __forceinline__ double rk_element(const double *__restrict__ mom,
     return v;
 }
 
-__global__ void k_rk_store(const double *__restrict__ mom, const double *__restrict__ dint,
-                          const double *__restrict__ tot, int k, int K1, int N, int n_iv,
-                          int64_t tile, int k_first, int k_count, double *__restrict__ R) {
-    const int W = 2 * k - 1, W2 = W * W;
-    const int a = blockIdx.x / N, b = blockIdx.x - a * N;
-    double *dst = R + (size_t)blockIdx.x * tile;
+// Tile t = a * N + b of the FP64 store (block-wide).
+__device__ void rk_tile_fp64(const RadialDev &P, int64_t t, int k_first, int k_count) {
+    const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
+    const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
+    double *dst = P.R + (size_t)t * P.tile;
     const int nel = K1 * W2;
-    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+    for (int e = threadIdx.x; e < P.tile; e += blockDim.x) {
         if (e >= nel) {
             dst[e] = 0.0;
             continue;
@@ -267,24 +281,21 @@ __global__ void k_rk_store(const double *__restrict__ mom, const double *__restr
         int kk = e / W2, rem = e - kk * W2;
         if (kk < k_first || kk >= k_first + k_count) continue;
         int dc = rem / W, dd = rem - dc * W;
-        dst[e] = rk_element(mom, dint, tot, k, K1, N, n_iv, a, b, kk, dc, dd);
+        dst[e] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk, dc, dd);
     }
 }
 
-__global__ void k_rk_store_mixed(const double *__restrict__ mom, const double *__restrict__ dint,
-                                const double *__restrict__ tot, int k, int K1, int N, int n_iv,
-                                int64_t tile, int k_first, int k_count, float2 *__restrict__ Rf,
-                                int *__restrict__ Rexp) {
-    extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile
-    __shared__ int sexp[kMaxK1];
-    const int W = 2 * k - 1, W2 = W * W;
-    const int a = blockIdx.x / N, b = blockIdx.x - a * N;
+// Tile t of the mixed store (block-wide); sv holds K1 W^2 doubles.
+__device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_count,
+                              double *sv, int *sexp) {
+    const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
+    const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
     const int nel = K1 * W2;
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
         int kk = e / W2, rem = e - kk * W2;
         if (kk < k_first || kk >= k_first + k_count) continue;
         int dc = rem / W, dd = rem - dc * W;
-        sv[e] = rk_element(mom, dint, tot, k, K1, N, n_iv, a, b, kk, dc, dd);
+        sv[e] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk, dc, dd);
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -295,12 +306,12 @@ __global__ void k_rk_store_mixed(const double *__restrict__ mom, const double *_
         int ex = (m > 0.0) ? ilogb(m) : 0;
         if (lane == 0) {
             sexp[kk] = ex;
-            Rexp[(size_t)blockIdx.x * K1 + kk] = ex;
+            P.Rexp[(size_t)t * K1 + kk] = ex;
         }
     }
     __syncthreads();
-    float2 *dst = Rf + (size_t)blockIdx.x * tile;
-    for (int e = threadIdx.x; e < tile; e += blockDim.x) {
+    float2 *dst = P.Rf + (size_t)t * P.tile;
+    for (int e = threadIdx.x; e < P.tile; e += blockDim.x) {
         if (e >= nel) {
             dst[e] = make_float2(0.f, 0.f);
             continue;
@@ -312,6 +323,78 @@ __global__ void k_rk_store_mixed(const double *__restrict__ mom, const double *_
         float hi = __double2float_rn(x);
         float lo = __double2float_rn(x - (double)hi);
         dst[e] = make_float2(hi, lo);
+    }
+}
+
+__global__ void k_rk_store(RadialDev P, int k_first, int k_count) {
+    rk_tile_fp64(P, blockIdx.x, k_first, k_count);
+}
+
+__global__ void k_rk_store_mixed(RadialDev P, int k_first, int k_count) {
+    extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile
+    __shared__ int sexp[kMaxK1];
+    rk_tile_mixed(P, blockIdx.x, k_first, k_count, sv, sexp);
+}
+
+// ---------------------------------------------------------------------------
+// Batched radial stage: one persistent kernel per stage runs that stage of
+// every problem of a batch.  Items [off[p], off[p+1]) belong to problem p
+// (0: intervals, 1: (interval, multipole), 2: chunks of blockDim totals,
+// 3: R^k tiles); a CTA takes `chunk` consecutive items per atomicAdd on the
+// stage's counter until the queue is empty.  No CTA waits on another.
+// ---------------------------------------------------------------------------
+struct BatchStage {
+    const RadialDev *probs;
+    const int64_t *off;  // [n + 1]
+    int n, chunk;
+    unsigned long long *counter;
+};
+
+__device__ __forceinline__ int find_problem(const int64_t *off, int n, int64_t it) {
+    int lo = 0, hi = n - 1;  // largest p with off[p] <= it
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= it)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int STAGE>
+__global__ void k_radial_batch(BatchStage B) {
+    extern __shared__ double sm[];
+    __shared__ int sexp[kMaxK1];
+    __shared__ unsigned long long s_it;
+    const int64_t total = B.off[B.n];
+    for (;;) {
+        if (threadIdx.x == 0) s_it = atomicAdd(B.counter, (unsigned long long)B.chunk);
+        __syncthreads();
+        const int64_t it0 = (int64_t)s_it;
+        __syncthreads();
+        if (it0 >= total) break;
+        const int64_t it1 = min(it0 + (int64_t)B.chunk, total);
+        for (int64_t it = it0; it < it1; ++it) {
+            const int p = find_problem(B.off, B.n, it);
+            const RadialDev P = B.probs[p];
+            const int64_t li = it - B.off[p];
+            if (STAGE == 0) {
+                tabulate_iv(P, (int)li);
+            } else if (STAGE == 1) {
+                moments_item(P, (int)(li / P.K1), (int)(li % P.K1), sm);
+                __syncthreads();  // shared arrays are rewritten by the next item
+            } else if (STAGE == 2) {
+                const int64_t e = li * blockDim.x + threadIdx.x;
+                if (e < totals_count(P)) totals_elem(P, e);
+            } else {
+                if (P.mixed)
+                    rk_tile_mixed(P, li, 0, P.K1, sm, sexp);
+                else
+                    rk_tile_fp64(P, li, 0, P.K1);
+                __syncthreads();
+            }
+        }
     }
 }
 
@@ -341,6 +424,35 @@ __global__ void k_rk_gather(const double *__restrict__ R, const float2 *__restri
             }
         }
         vals[e] = v;
+    }
+}
+
+// Multipole kk of the whole store as doubles, out[a][b][c-a+k-1][d-b+k-1]
+// (0-based a, b; zero where c or d falls outside the basis).
+__global__ void k_rk_slice(const double *__restrict__ R, const float2 *__restrict__ Rf,
+                           const int *__restrict__ Rexp, int kk, int k, int K1, int N,
+                           int64_t tile, double *__restrict__ out) {
+    const int W = 2 * k - 1;
+    const int64_t n = (int64_t)N * N * W * W;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = e / (W * W);
+        const int r = (int)(e - t * W * W), dc = r / W, dd = r - dc * W;
+        const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
+        const int c = a + dc - (k - 1), d = b + dd - (k - 1);
+        double v = 0.0;
+        if (c >= 0 && c < N && d >= 0 && d < N) {
+            const size_t o = (size_t)t * tile + ((size_t)kk * W + dc) * W + dd;
+            if (R) {
+                v = R[o];
+            } else {
+                const float2 x = Rf[o];
+                const int ex = Rexp[(size_t)t * K1 + kk];
+                v = ((double)x.x + (double)x.y) *
+                    __longlong_as_double((long long)(1023 - kRkBias + ex) << 52);
+            }
+        }
+        out[e] = v;
     }
 }
 
@@ -422,11 +534,37 @@ static inline unsigned grid_for(int64_t n, int threads) {
     return (unsigned)g;
 }
 
+RadialDev radial_dev(const bs2e_handle *h) {
+    const Radial &g = h->g;
+    RadialDev P;
+    P.knots = h->d_knots;
+    P.glx = h->d_glx;
+    P.glw = h->d_glw;
+    P.tab_r = h->d_tab_r;
+    P.tab_B = h->d_tab_B;
+    P.tab_D2 = h->d_tab_D2;
+    P.tab_D1 = h->d_tab_D1;
+    P.tab_ri = h->d_tab_ri;
+    P.tab_Bi = h->d_tab_Bi;
+    P.mom = h->d_mom;
+    P.dint = h->d_dint;
+    P.tot = h->d_tot;
+    P.R = h->d_R;
+    P.Rf = h->d_Rf;
+    P.Rexp = h->d_Rexp;
+    P.k = g.k;
+    P.q = g.q;
+    P.K1 = g.K1;
+    P.N = g.N;
+    P.n_iv = g.n_iv;
+    P.mixed = h->precision == BS2E_PREC_MIXED ? 1 : 0;
+    P.tile = g.tile;
+    return P;
+}
+
 void launch_tabulate(bs2e_handle *h) {
     const Radial &g = h->g;
-    k_tabulate<<<g.n_iv, 128, 0, h->stream>>>(h->d_knots, h->d_glx, g.k, g.q, h->d_tab_r,
-                                               h->d_tab_B, h->d_tab_D2, h->d_tab_D1, h->d_tab_ri,
-                                               h->d_tab_Bi);
+    k_tabulate<<<g.n_iv, 128, 0, h->stream>>>(radial_dev(h));
     h->launches++;
 }
 
@@ -440,16 +578,14 @@ void launch_moments(bs2e_handle *h) {
     size_t smem = moments_smem(g);
     cudaFuncSetAttribute(k_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid(g.n_iv, g.K1);
-    k_moments<<<grid, 256, smem, h->stream>>>(h->d_knots, h->d_glw, g.k, g.q, g.K1, h->d_tab_r,
-                                              h->d_tab_B, h->d_tab_ri, h->d_tab_Bi, h->d_mom,
-                                              h->d_dint);
+    k_moments<<<grid, 256, smem, h->stream>>>(radial_dev(h));
     h->launches++;
 }
 
 void launch_totals(bs2e_handle *h) {
     const Radial &g = h->g;
     int64_t n = (int64_t)2 * g.K1 * g.N * g.W;
-    k_totals<<<grid_for(n, 256), 256, 0, h->stream>>>(h->d_mom, g.k, g.K1, g.N, g.n_iv, h->d_tot);
+    k_totals<<<grid_for(n, 256), 256, 0, h->stream>>>(radial_dev(h));
     h->launches++;
 }
 
@@ -459,20 +595,63 @@ void launch_rk_fill(bs2e_handle *h, int k_first, int k_count) {
     if (h->precision == BS2E_PREC_MIXED) {
         size_t smem = (size_t)g.K1 * g.W * g.W * sizeof(double);
         cudaFuncSetAttribute(k_rk_store_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_rk_store_mixed<<<tiles, 256, smem, h->stream>>>(h->d_mom, h->d_dint, h->d_tot, g.k, g.K1,
-                                                         g.N, g.n_iv, g.tile, k_first, k_count,
-                                                         h->d_Rf, h->d_Rexp);
+        k_rk_store_mixed<<<tiles, 256, smem, h->stream>>>(radial_dev(h), k_first, k_count);
     } else {
-        k_rk_store<<<tiles, 256, 0, h->stream>>>(h->d_mom, h->d_dint, h->d_tot, g.k, g.K1, g.N,
-                                                g.n_iv, g.tile, k_first, k_count, h->d_R);
+        k_rk_store<<<tiles, 256, 0, h->stream>>>(radial_dev(h), k_first, k_count);
     }
     h->launches++;
+}
+
+static const void *batch_kernel(int stage) {
+    switch (stage) {
+        case 0: return (const void *)k_radial_batch<0>;
+        case 1: return (const void *)k_radial_batch<1>;
+        case 2: return (const void *)k_radial_batch<2>;
+        default: return (const void *)k_radial_batch<3>;
+    }
+}
+
+int radial_batch_blocks_per_sm(int stage, int threads, size_t smem) {
+    cudaFuncSetAttribute(batch_kernel(stage), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, batch_kernel(stage), threads, smem) !=
+        cudaSuccess)
+        return 0;
+    return nb;
+}
+
+void launch_radial_batch(cudaStream_t s, int stage, int grid, int threads, size_t smem,
+                         const RadialDev *probs, const int64_t *off, int n,
+                         unsigned long long *counter, int chunk) {
+    BatchStage B;
+    B.probs = probs;
+    B.off = off;
+    B.n = n;
+    B.chunk = chunk;
+    B.counter = counter;
+    switch (stage) {
+        case 0: k_radial_batch<0><<<grid, threads, smem, s>>>(B); break;
+        case 1: k_radial_batch<1><<<grid, threads, smem, s>>>(B); break;
+        case 2: k_radial_batch<2><<<grid, threads, smem, s>>>(B); break;
+        default: k_radial_batch<3><<<grid, threads, smem, s>>>(B); break;
+    }
 }
 
 void launch_rk_gather(bs2e_handle *h, int64_t n, const int64_t *d_keys, double *d_vals) {
     const Radial &g = h->g;
     k_rk_gather<<<grid_for(n * g.K1, 256), 256, 0, h->stream>>>(
         h->d_R, h->d_Rf, h->d_Rexp, g.k, g.K1, g.N, g.tile, n, d_keys, d_vals);
+    h->launches++;
+}
+
+void launch_rk_slice(bs2e_handle *h, int kk, double *d_out) {
+    const Radial &g = h->g;
+    const int64_t n = (int64_t)g.N * g.N * g.W * g.W;
+    const bool mixed = h->precision == BS2E_PREC_MIXED;
+    k_rk_slice<<<grid_for(n, 256), 256, 0, h->stream>>>(mixed ? nullptr : h->d_R, h->d_Rf,
+                                                        h->d_Rexp, kk, g.k, g.K1, g.N, g.tile,
+                                                        d_out);
     h->launches++;
 }
 

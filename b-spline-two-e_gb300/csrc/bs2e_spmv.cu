@@ -1,0 +1,112 @@
+// bs2e_spmv.cu -- products of the assembled CSR blocks with complex vectors.
+//
+// Reference: CSR_mv, CSR_T_mv and CSR_mv_sym (src/tools/sparse_array_tools.f90:
+// 966-1074), the mat-vecs the solvers apply to H and S (eig_tools.f90:327-373,
+// propagator_CN.f90:201-203, quasi_calcs.f90:838-871).  CSR_mv_sym calls
+// mkl_zcsrsymv('U'): A is complex symmetric (not Hermitian: the CAP makes H
+// complex symmetric) and only the entries with column >= row are read.
+//
+// One warp per row: lanes stride the row's entries, so the int64 column and
+// complex128 value loads of a warp are contiguous (256 B + 512 B per step), the
+// x gathers hit L1/L2 (columns of a row sit in a few narrow windows), and a
+// shuffle reduction gives y(row).  The transposed and symmetric products add
+// the scattered part with FP64 atomics into a zeroed y.  Every row pointer and
+// column index is range-checked against nnz / n_cols; a bad one sets the flag
+// word and is skipped, so malformed input reads nothing out of bounds.
+#include <cuda_runtime.h>
+
+#include "bs2e_internal.h"
+
+namespace bs2e {
+namespace {
+
+__device__ __forceinline__ void cmac(double &re, double &im, double2 a, double2 x) {
+    re = fma(a.x, x.x, re);
+    re = fma(-a.y, x.y, re);
+    im = fma(a.x, x.y, im);
+    im = fma(a.y, x.x, im);
+}
+
+// OP 0: y = A x.  OP 1: y += A^T x (y zeroed).  OP 2: y += U x + (U - diag)^T x
+// with U the column >= row part of A (y zeroed).
+template <int OP>
+__global__ void __launch_bounds__(256) k_csr_mv(int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                                const int64_t *__restrict__ ptr,
+                                                const int64_t *__restrict__ idx,
+                                                const double2 *__restrict__ A,
+                                                const double2 *__restrict__ x,
+                                                double2 *__restrict__ y, int *__restrict__ bad) {
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n_rows) return;  // warp-uniform
+    const int64_t j0 = ptr[row] - 1, j1 = ptr[row + 1] - 1;
+    if (j0 < 0 || j1 < j0 || j1 > nnz) {
+        if (lane == 0) atomicOr(bad, 1);
+        return;
+    }
+    double re = 0.0, im = 0.0;
+    const double2 xr = (OP != 0) ? x[row] : make_double2(0.0, 0.0);
+    for (int64_t j = j0 + lane; j < j1; j += 32) {
+        const int64_t c = idx[j] - 1;
+        const double2 a = A[j];
+        if (c < 0 || c >= n_cols) {
+            atomicOr(bad, 2);
+            continue;
+        }
+        if (OP == 1) {
+            double tr = 0.0, ti = 0.0;
+            cmac(tr, ti, a, xr);
+            atomicAdd(&y[c].x, tr);
+            atomicAdd(&y[c].y, ti);
+            continue;
+        }
+        if (OP == 2 && c < row) continue;
+        cmac(re, im, a, x[c]);
+        if (OP == 2 && c > row) {
+            double tr = 0.0, ti = 0.0;
+            cmac(tr, ti, a, xr);
+            atomicAdd(&y[c].x, tr);
+            atomicAdd(&y[c].y, ti);
+        }
+    }
+    if (OP == 1) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) {
+        if (OP == 0) {
+            y[row] = make_double2(re, im);
+        } else {
+            atomicAdd(&y[row].x, re);
+            atomicAdd(&y[row].y, im);
+        }
+    }
+}
+
+}  // namespace
+
+void launch_csr_mv(bs2e_handle *h, int op, int64_t n_rows, int64_t n_cols, int64_t nnz,
+                   const int64_t *ptr, const int64_t *idx, const double2 *A, const double2 *x,
+                   double2 *y, int *bad) {
+    if (op != 0) {
+        int64_t n_out = op == 1 ? n_cols : n_rows;
+        cudaMemsetAsync(y, 0, sizeof(double2) * (size_t)n_out, h->stream);
+    }
+    if (n_rows == 0) return;
+    const int threads = 256, rows_per_block = threads / 32;
+    const int64_t blocks = (n_rows + rows_per_block - 1) / rows_per_block;
+    if (op == 0)
+        k_csr_mv<0><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
+                                                                 x, y, bad);
+    else if (op == 1)
+        k_csr_mv<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
+                                                                 x, y, bad);
+    else
+        k_csr_mv<2><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
+                                                                 x, y, bad);
+    h->launches++;
+}
+
+}  // namespace bs2e

@@ -18,7 +18,8 @@ module bs2e_gpu
 
     type, bind(C) :: bs2e_opts_c
         integer(c_int64_t) :: precision, device
-        integer(c_int64_t) :: reserved(6)
+        integer(c_int64_t) :: stage_bytes    ! HBM staging per area for host-array fills (0 = 2 GiB)
+        integer(c_int64_t) :: reserved(5)
     end type bs2e_opts_c
 
     interface
@@ -96,6 +97,43 @@ module bs2e_gpu
             complex(c_double_complex), intent(out) :: H_data(*)
             integer(c_int64_t), intent(out) :: S_index_ptr(*), S_indices(*)
             complex(c_double_complex), intent(out) :: S_data(*)
+        end function
+
+        ! rows row_first .. row_first+row_count-1 (0-based first row) of a block,
+        ! range-local index_ptr; spin = 0 singlet, 1 triplet
+        integer(c_int32_t) function bs2e_block_count_rows(h, configs, n_config, L, spin, full, &
+                row_first, row_count, nnz_H, nnz_S) bind(C, name="bs2e_block_count_rows")
+            import :: c_int32_t, c_int64_t, c_ptr, bs2e_config_c
+            type(c_ptr), value :: h
+            type(bs2e_config_c), intent(in) :: configs(*)
+            integer(c_int64_t), value :: n_config, L, spin, full, row_first, row_count
+            integer(c_int64_t), intent(out) :: nnz_H, nnz_S
+        end function
+
+        integer(c_int32_t) function bs2e_block_fill_rows(h, configs, n_config, L, spin, full, &
+                row_first, row_count, H_index_ptr, H_indices, H_data, S_index_ptr, S_indices, &
+                S_data, out_on_device) bind(C, name="bs2e_block_fill_rows")
+            import :: c_int32_t, c_int64_t, c_double_complex, c_ptr, bs2e_config_c
+            type(c_ptr), value :: h
+            type(bs2e_config_c), intent(in) :: configs(*)
+            integer(c_int64_t), value :: n_config, L, spin, full, row_first, row_count
+            integer(c_int64_t), intent(out) :: H_index_ptr(*), H_indices(*)
+            complex(c_double_complex), intent(out) :: H_data(*)
+            integer(c_int64_t), intent(out) :: S_index_ptr(*), S_indices(*)
+            complex(c_double_complex), intent(out) :: S_data(*)
+            integer(c_int64_t), value :: out_on_device
+        end function
+
+        ! CSR_mv (op 0), CSR_T_mv (op 1), CSR_mv_sym (op 2) of a type(CSR_matrix)
+        integer(c_int32_t) function bs2e_csr_mv(h, op, n_rows, n_cols, nnz, index_ptr, indices, &
+                data, x, y, on_device) bind(C, name="bs2e_csr_mv")
+            import :: c_int32_t, c_int64_t, c_double_complex, c_ptr
+            type(c_ptr), value :: h
+            integer(c_int64_t), value :: op, n_rows, n_cols, nnz
+            integer(c_int64_t), intent(in) :: index_ptr(*), indices(*)
+            complex(c_double_complex), intent(in) :: data(*), x(*)
+            complex(c_double_complex), intent(out) :: y(*)
+            integer(c_int64_t), value :: on_device
         end function
     end interface
 

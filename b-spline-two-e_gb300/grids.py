@@ -48,3 +48,20 @@ def generate_grid(k, m, Z, h_max, r_max):
         g.append(g[-1] + Z * h_max)
     g.extend([g[-1]] * (k - 1))
     return np.asarray(g, dtype=np.float64) / Z
+
+
+def ragged_problems(n=64, seed=0):
+    """The ragged batch of radial problems: per problem, in this draw order
+    from numpy.random.default_rng(seed): order k from {6, 7, 8}, spline count
+    N uniform in [100, 500], max_k uniform in [4, 16], and the largest channel
+    l uniform in [0, 8] (it sizes the angular part only).  r_max = N a.u. on
+    the exp-linear grid, k_GL = k + 4 Gauss-Legendre points per interval."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        k = int(rng.choice([6, 7, 8]))
+        N = int(rng.integers(100, 501))
+        max_k = int(rng.integers(4, 17))
+        l_max = int(rng.integers(0, 9))
+        out.append(dict(k=k, n_b=N, r_max=float(N), k_GL=k + 4, max_k=max_k, l_max=l_max))
+    return out

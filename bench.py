@@ -11,9 +11,12 @@ value : R^k elements/s = P^2 (max_k+1) / step time, outputs written into
         device buffers (inputs resident).  P = ordered band pairs = 2,558.
 e2e   : same metric through the C ABI with host output buffers (pinned): the
         configuration lists go host->device and every CSR block device->host.
-roofline: the CSR fill kernel (k_fill), timed with CUDA events on the
+roofline: the CSR fill kernel (k_csr_fill), timed with CUDA events on the
         library's stream; algorithmic bytes = 24 B per stored H/S entry
-        (int64 index + complex128 value) + the R^k tiles it stages.
+        (int64 index + complex128 value) + the R^k tiles it stages.  traffic:
+        DRAM bytes per launch, from the ncu capture of block 0 (profiles/
+        k_csr_fill_config2_block0.md) scaled to the average launch by
+        algorithmic bytes.
 cpu_baseline: the CPU oracle (C restatement of the reference, OpenMP) on a
         bounded sample: full Slater primitives + R^k map, and a row sample of
         every block extrapolated to the full block (one thread per block, the
@@ -24,6 +27,10 @@ python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 python bench.py --profile-block B   one radial pass and one count + fill of block B
                                     (0 = L=0 singlet, 117,620 rows): the small case
                                     for ncu captures of the fill kernel
+python bench.py --workload batch    the ragged batch of 64 radial problems
+                                    (tests/golden/ragged_problems.json): batched,
+                                    graph-captured radial stage vs the same 64
+                                    problems one handle after another
 """
 import argparse
 import json
@@ -40,6 +47,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 METRIC = "R^k elements/s + 2e-H assembly s, mixed vs FP64 on GB300 at ≤1e-9 rel err"
 WORKLOAD = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5, max_L=3, Z=2, spins=(0, 1),
                 full=True, cap_order=2, cap_r0=10.0, cap_eta=1e-3)
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of the k_csr_fill launch on
+# block 0 (ncu --set full, profiles/k_csr_fill_config2_block0.md) and that
+# launch's algorithmic bytes (3,154,438,224 B of CSR + 20,100 staged tiles).
+NCU_BLOCK0_DRAM = {"fp64": 3516823112.0, "mixed": 3518698768.0}
+NCU_BLOCK0_ALG = 3453526224.0
 
 
 def _pkg():
@@ -250,6 +264,9 @@ def run_ours(args, rank, world):
     launches = h.launch_count - launches0
     t_dev = ev0.elapsed_time(ev1) / 1e3
     fill_s = sum(a.elapsed_time(b) for a, b in fill_ms) / 1e3
+    nb = len(blocks)
+    per_block_ms = [sum(fill_ms[i][0].elapsed_time(fill_ms[i][1])
+                        for i in range(j, len(fill_ms), nb)) / args.steps for j in range(nb)]
     t_dev = _max_over_ranks(t_dev, world)
     P = band_pairs(w["k"], w["n_b"])
     elems = P * P * (w["max_k"] + 1)
@@ -267,7 +284,7 @@ def run_ours(args, rank, world):
 
     if args.no_e2e:
         return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, None,
-                       launches, fill_bytes, fill_s, clk, h, rank)
+                       launches, fill_bytes, fill_s, clk, h, rank, per_block_ms)
     # e2e through the C ABI with pinned host buffers
     del out_dev
     torch.cuda.empty_cache()
@@ -303,15 +320,18 @@ def run_ours(args, rank, world):
     e2e = {"value": world * elems / t_e2e, "unit": "R^k elements/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "s_per_step": t_e2e}
     return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
-                   fill_bytes, fill_s, clk, h, rank)
+                   fill_bytes, fill_s, clk, h, rank, per_block_ms)
 
 
 def _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
-            fill_bytes, fill_s, clk, h, rank):
+            fill_bytes, fill_s, clk, h, rank, per_block_ms):
     w = WORKLOAD
     value = world * elems * args.steps / t_dev
     peak, peak_src = _peaks()
     achieved = fill_bytes * args.steps / fill_s / 1e9 if fill_s > 0 else None
+    # DRAM bytes of an average fill launch: block 0's measured traffic per
+    # algorithmic byte times the average launch's algorithmic bytes
+    traffic = NCU_BLOCK0_DRAM[args.precision] / NCU_BLOCK0_ALG * fill_bytes / len(blocks)
     res = {
         "metric": METRIC, "value": value, "unit": "R^k elements/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
@@ -329,11 +349,13 @@ def _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e,
         "rk_stage_elements_per_s": elems / t_radial,
         "e2e": e2e,
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "k_fill", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "k_csr_fill", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": None, "peak_source": peak_src,
-                     "algorithmic_bytes_per_step": int(fill_bytes),
-                     "fill_s_per_step": fill_s / args.steps},
+                     "traffic": traffic, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": fill_bytes / len(blocks),
+                     "launches_per_step": len(blocks),
+                     "fill_s_per_step": fill_s / args.steps,
+                     "fill_ms_per_block": per_block_ms},
         "clocks": clk.summary(),
     }
     h.close()
@@ -373,6 +395,146 @@ def profile_block(args):
         print(json.dumps({"profile_block": args.profile_block, "L": L, "spin": spin,
                           "rows": int(n), "nnz_H": ch, "nnz_S": cs,
                           "output_bytes": 24 * (ch + cs)}))
+
+
+def run_batch(args):
+    """The ragged batch of 64 radial problems: the batched, graph-captured
+    radial stage (bs2e_batch_run) against the same handles run one after
+    another through bs2e_slater + bs2e_rk; both produce bit-identical stores."""
+    import torch
+    pkg = _pkg()
+    probs = json.load(open(os.path.join(ROOT, "tests", "golden", "ragged_problems.json")))
+    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
+    hs = [pkg.Bs2e(pkg.grids.explin_knots(p["k"], p["n_b"], p["r_max"]), p["k"], p["k_GL"],
+                   p["max_k"], precision=prec) for p in probs]
+    elems = sum(band_pairs(p["k"], p["n_b"]) ** 2 * (p["max_k"] + 1) for p in probs)
+    store_bytes = sum(p["n_b"] ** 2 * (((p["max_k"] + 1) * (2 * p["k"] - 1) ** 2 + 1) // 2 * 2) * 8
+                      for p in probs)
+
+    def fingerprint(sel):
+        out = []
+        for i in sel:
+            h = hs[i]
+            W = 2 * h.k - 1
+            buf = torch.empty(h.n_b * h.n_b * W * W, dtype=torch.float64, device="cuda")
+            acc = 0
+            for kk in range(h.K1):
+                h.rk_export(kk, buf.data_ptr(), on_device=True)
+                acc ^= int(buf.view(torch.int64).sum().item()) & ((1 << 63) - 1)
+            out.append(acc)
+        return out
+
+    sel = [0, len(hs) // 2, len(hs) - 1]
+    batch = pkg.RadialBatch(hs)
+    t0 = time.perf_counter()
+    batch.run()  # tuning + graph capture
+    t_first = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        batch.run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.run()
+    t_batch = (time.perf_counter() - t0) / args.steps
+    fp_batch = fingerprint(sel)
+    for _ in range(args.warmup):
+        for h in hs:
+            h.slater()
+            h.rk()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for h in hs:
+            h.slater()
+            h.rk()
+    t_seq = (time.perf_counter() - t0) / args.steps
+    fp_seq = fingerprint(sel)
+    tun = batch.tuning()
+    batch.close()
+    for h in hs:
+        h.close()
+    return {
+        "metric": "R^k elements/s, ragged batch of 64 radial problems", "impl": "ours",
+        "value": elems / t_batch, "unit": "R^k elements/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_batch, "higher_is_better": True,
+        "dtype": "f64" if prec == pkg.PREC_FP64 else "f64 sums, f32-pair store",
+        "data": "synthetic: 64 problems from numpy default_rng(0), tests/golden/ragged_problems.json",
+        "config": {"workload": "ragged batch: order in {6,7,8}, N in [100,500], r_max=N, "
+                               "max_k in [4,16], k_GL=k+4", "rk_elements_per_step": elems,
+                   "store_bytes": store_bytes, "timing": "wall clock, each run synchronised"},
+        "sequential": {"value": elems / t_seq, "ms_per_step": 1e3 * t_seq,
+                       "launches_per_step": 4 * len(hs)},
+        "speedup_vs_sequential": t_seq / t_batch,
+        "first_run_s": t_first, "tuning": tun,
+        "bit_identical_sample": fp_batch == fp_seq,
+    }
+
+
+def run_matvec(args):
+    """CSR_mv / CSR_mv_sym (bs2e_csr_mv on device pointers) over the H blocks of
+    the bench workload, assembled into HBM by the library: achieved GB/s of
+    the mat-vec kernel against the measured copy bandwidth."""
+    import torch
+    pkg = _pkg()
+    w = WORKLOAD
+    dev = torch.device("cuda", 0)
+    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    blocks = workload_blocks(pkg, w)
+    res = {}
+    with pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec) as h:
+        h.slater()
+        h.rk()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+        stream = torch.cuda.ExternalStream(h.stream, device=dev)
+        for op, full, name in ((0, True, "csr_mv"), (2, False, "csr_mv_sym")):
+            t_ms, nbytes, nnz_all = 0.0, 0, 0
+            for (L, par, spin, cf) in blocks[:4]:
+                nH, nS = h.block_count(cf, L, full, spin)
+                n = cf.size
+                ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
+                idx = torch.empty(nH, dtype=torch.int64, device=dev)
+                dat = torch.empty(nH, dtype=torch.complex128, device=dev)
+                sp = torch.empty(n + 1, dtype=torch.int64, device=dev)
+                si = torch.empty(nS, dtype=torch.int64, device=dev)
+                sd = torch.empty(nS, dtype=torch.complex128, device=dev)
+                h.block_fill_into(cf, L, full, spin,
+                                  dict(index_ptr=ptr.data_ptr(), indices=idx.data_ptr(),
+                                       data=dat.data_ptr()),
+                                  dict(index_ptr=sp.data_ptr(), indices=si.data_ptr(),
+                                       data=sd.data_ptr()), on_device=True)
+                del si, sd, sp
+                x = torch.randn(n, dtype=torch.complex128, device=dev)
+                y = torch.empty(n, dtype=torch.complex128, device=dev)
+                args_ = (op, n, n, nH, ptr.data_ptr(), idx.data_ptr(), dat.data_ptr(),
+                         x.data_ptr(), y.data_ptr())
+                for _ in range(args.warmup):
+                    h.csr_mv_device(*args_)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(stream)
+                for _ in range(args.steps):
+                    h.csr_mv_device(*args_)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t_ms += e0.elapsed_time(e1) / args.steps
+                # algorithmic bytes: int64 column + complex128 value per entry,
+                # two row pointers per row, x read once and y written once
+                nbytes += 24 * nH + 8 * (n + 1) + 32 * n
+                nnz_all += nH
+                del ptr, idx, dat, x, y
+                torch.cuda.empty_cache()
+            peak, src = _peaks()
+            gbs = nbytes / (t_ms / 1e3) / 1e9
+            res[name] = {"ms_per_product_all_blocks": t_ms, "nnz": nnz_all, "bytes": nbytes,
+                         "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak,
+                         "peak_source": src}
+    return {"metric": "H x: CSR mat-vec over the L=0..3 singlet H blocks", "results": res,
+            "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 singlet",
+                       "precision_of_blocks": args.precision},
+            "steps": args.steps, "warmup": args.warmup}
 
 
 def _max_over_ranks(x, world):
@@ -421,9 +583,16 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-block", type=int, default=None)
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch", "matvec"])
     args = ap.parse_args()
     if args.profile_block is not None:
         profile_block(args)
+        return
+    if args.workload == "batch":
+        print(json.dumps(run_batch(args)), flush=True)
+        return
+    if args.workload == "matvec":
+        print(json.dumps(run_matvec(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

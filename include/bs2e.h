@@ -64,7 +64,9 @@ typedef struct bs2e_handle bs2e_handle;
 typedef struct {
     int64_t precision; /* BS2E_PREC_FP64 (default) or BS2E_PREC_MIXED */
     int64_t device;    /* CUDA device ordinal (default 0) */
-    int64_t reserved[6];
+    int64_t stage_bytes; /* size of each of the two HBM staging areas of fills
+                            into host arrays (0 = 2 GiB) */
+    int64_t reserved[5];
 } bs2e_opts;
 
 /* One two-electron configuration: type(config) of src/tools/orbital_tools.f90:15-19
@@ -119,6 +121,14 @@ BS2E_API bs2e_status bs2e_rk_get(bs2e_handle *h, const int64_t key[4], double *v
 /* Batched bs2e_rk_get: keys is 4 x n column-major, vals is (max_k+1) x n. */
 BS2E_API bs2e_status bs2e_rk_get_batch(bs2e_handle *h, int64_t n, const int64_t *keys,
                                        double *vals);
+
+/* Multipole k of the whole R^k store as doubles, out[a][b][c-a+k_o-1][d-b+k_o-1]
+ * (C order, N*N*W*W values, W = 2*k_o-1, k_o the spline order, 0-based a, b;
+ * zero where c or d falls outside the basis).  The mixed store is returned as
+ * the exact double value of its scaled FP32 pair.  on_device = 1: out is a
+ * device pointer.  For dumps and precision studies; Nd_DOK offers only
+ * get_val (sparse_array_tools.f90:536-555). */
+BS2E_API bs2e_status bs2e_rk_export(bs2e_handle *h, int64_t k, double *out, int64_t on_device);
 
 /* bs2e_rk_get_batch without any device allocation.  This entry point has no
  * counterpart in the reference.  It is for callers that can't allocate device
@@ -251,6 +261,85 @@ BS2E_API bs2e_status bs2e_write_block(const char *path, int64_t n_rows_b, int64_
                                       const int64_t *const *index_ptr,
                                       const int64_t *const *indices, const double *const *data,
                                       int64_t max_subrecord);
+
+/* Row ranges of a block, for blocks too large to hold at once: the same
+ * configuration list, L, spin and full as bs2e_block_count_ex, and rows
+ * [row_first, row_first + row_count).  count_rows returns the range's
+ * non-zeros; fill_rows writes the range's CSR arrays with a range-local
+ * 1-based index_ptr (row_count + 1 entries, index_ptr[0] = 1) and the block's
+ * 1-based column indices, exactly the rows row_first.. of bs2e_block_fill_ex.
+ * With host outputs (out_on_device = 0), here and in bs2e_block_fill[_ex],
+ * the rows are assembled in chunks through two staging areas of at most
+ * 2 GiB each in HBM, the device-to-host copy of one chunk overlapping the
+ * assembly of the next.  No counterpart in the reference (its blocks are
+ * built whole, hamiltonian.f90:106-283). */
+BS2E_API bs2e_status bs2e_block_count_rows(bs2e_handle *h, const bs2e_config *configs,
+                                           int64_t n_config, int64_t L, int64_t spin,
+                                           int64_t full, int64_t row_first, int64_t row_count,
+                                           int64_t *nnz_H, int64_t *nnz_S);
+BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *configs,
+                                          int64_t n_config, int64_t L, int64_t spin, int64_t full,
+                                          int64_t row_first, int64_t row_count,
+                                          int64_t *H_index_ptr, int64_t *H_indices,
+                                          double *H_data, int64_t *S_index_ptr,
+                                          int64_t *S_indices, double *S_data,
+                                          int64_t out_on_device);
+
+/* Product of a 1-based CSR matrix (n_rows x n_cols, nnz entries, complex128
+ * data) with a complex128 vector, as the solvers apply H and S:
+ *   op 0: y = A x             CSR_mv     (src/tools/sparse_array_tools.f90:966-994)
+ *   op 1: y = A^T x           CSR_T_mv   (:996-1031), no conjugation
+ *   op 2: y = A x, A complex symmetric from its column >= row entries
+ *                             CSR_mv_sym (:1033-1074, mkl_zcsrsymv 'U')
+ * x has n_cols entries (n_rows for op 1), y n_rows (n_cols for op 1).
+ * on_device = 1: every pointer is a CUDA device pointer on the handle's
+ * device (e.g. blocks kept in HBM by bs2e_block_fill_ex); 0: host arrays,
+ * staged through the handle's buffers.  Row pointers and column indices are
+ * range-checked on the device (BS2E_ERR_ARG); the call returns when y is
+ * complete.  Sums run in a different order from the reference's, so y agrees
+ * with it to rounding (about 1e-16 of sum |a_ij x_j|). */
+BS2E_API bs2e_status bs2e_csr_mv(bs2e_handle *h, int64_t op, int64_t n_rows, int64_t n_cols,
+                                 int64_t nnz, const int64_t *index_ptr, const int64_t *indices,
+                                 const double *data, const double *x, double *y,
+                                 int64_t on_device);
+
+/* One CSR matrix from an n_rb x n_cb block matrix of 1-based CSR blocks, as
+ * CS_from_block / CSR_from_block do (src/tools/block_tools.f90:153-234): block
+ * (i, j) (0-based) is entry b = i + n_rb*j of shapes (rows, cols pairs), nnz,
+ * index_ptr, indices and data (complex128); blocks with nnz = 0 need no
+ * arrays.  Row r of block row i is the concatenation over j of row r of
+ * block (i, j), columns shifted by the widths of blocks (i, 0..j-1).  The
+ * output has sum(rows of block (i, 0)) rows and sum(nnz) entries, sized by
+ * the caller.  A block-diagonal matrix (CSR_from_block_diag, :289-348) is the
+ * case with empty off-diagonal blocks of the right shapes.  on_device = 1:
+ * the per-block pointers and the outputs are device pointers. */
+BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t n_cb,
+                                          const int64_t *shapes, const int64_t *nnz,
+                                          const int64_t *const *index_ptr,
+                                          const int64_t *const *indices,
+                                          const double *const *data, int64_t *out_index_ptr,
+                                          int64_t *out_indices, double *out_data,
+                                          int64_t on_device);
+
+/* Batched radial stage: bs2e_slater + bs2e_rk (every multipole) of n handles
+ * -- bases of different order, spline count, knots, quadrature and multipole
+ * range -- as four persistent kernels (tabulation, moments, pair totals, R^k
+ * store) that each drain one work queue over all problems, largest R^k
+ * store first.  The first bs2e_batch_run tunes the R^k kernel's threads per
+ * CTA and queue grab size by timing each candidate (every candidate is a
+ * complete pass) and captures the four stages in a CUDA graph; later runs
+ * replay the graph.  After a run every handle is in the state bs2e_slater +
+ * bs2e_rk(h, 0, max_k + 1) leaves it in, with bit-identical values.  The
+ * handles must be distinct, on one device, and outlive the batch; the run
+ * locks all of them.  No counterpart in the reference (one basis per
+ * basis_setup run, mat_els.f90:172-292, sparse_array_tools.f90:452-493). */
+typedef struct bs2e_batch bs2e_batch;
+BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, bs2e_batch **out);
+BS2E_API bs2e_status bs2e_batch_run(bs2e_batch *b);
+/* The tuned R^k shape, whether the graph exists, and kernels launched so far. */
+BS2E_API bs2e_status bs2e_batch_tuning(const bs2e_batch *b, int64_t *rk_threads, int64_t *chunk,
+                                       int64_t *graph_ready, int64_t *launches);
+BS2E_API bs2e_status bs2e_batch_destroy(bs2e_batch *b);
 
 /* The CUDA stream all work of the handle runs on (cudaStream_t as void*), the
  * number of kernels the handle has launched so far, and a full synchronize. */

@@ -851,3 +851,79 @@ int64_t or_dip_block(const or_config *rows, int64_t n_rows, int64_t L1, int64_t 
     }
     return p - 1;
 }
+
+/* ---- sparse_array_tools.f90:966-1074: CSR_mv, CSR_T_mv, CSR_mv_sym ------ */
+void or_csr_mv(int64_t op, int64_t n_rows, int64_t n_cols, const int64_t *ptr,
+               const int64_t *idx, const double *data, const double *x, double *y,
+               double *scale) {
+    const double complex *A = (const double complex *)data;
+    const double complex *X = (const double complex *)x;
+    double complex *Y = (double complex *)y;
+    int64_t n_out = op == 1 ? n_cols : n_rows;
+    for (int64_t i = 0; i < n_out; ++i) {
+        Y[i] = 0.0;
+        if (scale) scale[i] = 0.0;
+    }
+    if (op == 0) {
+        /* y(i) = y(i) + A%data(j)*x(A%indices(j)), j ascending (:987-992) */
+        for (int64_t i = 0; i < n_rows; ++i) {
+            double complex acc = 0.0;
+            for (int64_t j = ptr[i] - 1; j < ptr[i + 1] - 1; ++j) {
+                acc = acc + A[j] * X[idx[j] - 1];
+                if (scale) scale[i] += cabs(A[j]) * cabs(X[idx[j] - 1]);
+            }
+            Y[i] = acc;
+        }
+    } else if (op == 1) {
+        /* y(A%indices(j)) = y(A%indices(j)) + A%data(j)*x(i) (:1022-1027) */
+        for (int64_t i = 0; i < n_rows; ++i)
+            for (int64_t j = ptr[i] - 1; j < ptr[i + 1] - 1; ++j) {
+                Y[idx[j] - 1] += A[j] * X[i];
+                if (scale) scale[idx[j] - 1] += cabs(A[j]) * cabs(X[i]);
+            }
+    } else {
+        /* mkl_zcsrsymv('U') (:1053): the upper triangle (column >= row) of a
+         * complex symmetric A; the commented loop of :1057-1072 spells it out
+         * for upper-stored rows */
+        for (int64_t i = 0; i < n_rows; ++i)
+            for (int64_t j = ptr[i] - 1; j < ptr[i + 1] - 1; ++j) {
+                int64_t c = idx[j] - 1;
+                if (c < i) continue;
+                Y[i] += A[j] * X[c];
+                if (scale) scale[i] += cabs(A[j]) * cabs(X[c]);
+                if (c > i) {
+                    Y[c] += A[j] * X[i];
+                    if (scale) scale[c] += cabs(A[j]) * cabs(X[i]);
+                }
+            }
+    }
+}
+
+/* ---- block_tools.f90:188-234: CSR_from_block ---------------------------- */
+int64_t or_csr_from_blocks(int64_t n_rb, int64_t n_cb, const int64_t *shapes, const int64_t *nnz,
+                           const int64_t *const *ptr, const int64_t *const *idx,
+                           const double *const *data, int64_t *out_ptr, int64_t *out_idx,
+                           double *out_data) {
+    int64_t p = 1, row = 0;
+    for (int64_t i = 0; i < n_rb; ++i) {
+        for (int64_t ri = 0; ri < shapes[2 * i]; ++ri) {
+            int64_t col = 0;
+            row += 1;
+            out_ptr[row - 1] = p;
+            for (int64_t j = 0; j < n_cb; ++j) {
+                int64_t b = i + n_rb * j;
+                if (nnz[b] > 0) { /* arrays_allocated() */
+                    int64_t start = ptr[b][ri], end = ptr[b][ri + 1] - 1;
+                    for (int64_t e = start; e <= end; ++e, ++p) {
+                        out_idx[p - 1] = col + idx[b][e - 1];
+                        out_data[2 * (p - 1)] = data[b][2 * (e - 1)];
+                        out_data[2 * (p - 1) + 1] = data[b][2 * (e - 1) + 1];
+                    }
+                }
+                col += shapes[2 * b + 1];
+            }
+        }
+    }
+    out_ptr[row] = p;
+    return p - 1;
+}

@@ -109,6 +109,25 @@ int64_t or_dip_block(const or_config *rows, int64_t n_rows, int64_t L1, int64_t 
                      const double *S, const double *r_mat, const double *dr_mat,
                      const double *r_inv_mat, int64_t *ptr, int64_t *idx, double *data);
 
+/* Sparse products of a 1-based CSR matrix with a complex vector
+ * (src/tools/sparse_array_tools.f90:966-1074): op 0 = CSR_mv (y = A x),
+ * op 1 = CSR_T_mv (y = A^T x, no conjugation), op 2 = CSR_mv_sym, i.e.
+ * mkl_zcsrsymv('U'): A complex symmetric, only entries with column >= row
+ * used.  data, x, y complex128 interleaved; scale (optional) receives
+ * sum |a_ij| |x_j| per output entry. */
+void or_csr_mv(int64_t op, int64_t n_rows, int64_t n_cols, const int64_t *ptr,
+               const int64_t *idx, const double *data, const double *x, double *y,
+               double *scale);
+
+/* CSR_from_block (src/tools/block_tools.f90:188-234): block (i, j) of the
+ * n_rb x n_cb block matrix is b = i + n_rb*j; rows of block row i from block
+ * (i, 0); arrays of empty blocks are not read.  out_ptr has sum(rows) + 1
+ * entries; returns the number of entries written. */
+int64_t or_csr_from_blocks(int64_t n_rb, int64_t n_cb, const int64_t *shapes, const int64_t *nnz,
+                           const int64_t *const *ptr, const int64_t *const *idx,
+                           const double *const *data, int64_t *out_ptr, int64_t *out_idx,
+                           double *out_data);
+
 #ifdef __cplusplus
 }
 #endif

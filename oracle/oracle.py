@@ -54,6 +54,8 @@ def lib():
         "or_setup_radial_dip": (None, [p, i64, i64, i64, i64, p, p, p]),
         "or_dip_block": (i64, [p, i64, i64, i64, i64, p, i64, i64, i64, i64, i64, i64, i64, i64,
                                i64, p, p, p, p, p, p, p]),
+        "or_csr_mv": (None, [i64, i64, i64, p, p, p, p, p, p]),
+        "or_csr_from_blocks": (i64, [i64, i64, p, p, p, p, p, p, p, p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -215,3 +217,43 @@ def dip_block(rows, sym1, cols, sym2, q, compute, k, n_b, gauge, S, mats):
              data=np.zeros(n, np.complex128), nnz=n)
     lib().or_dip_block(*a, _p(D["index_ptr"]), _p(D["indices"]), _p(D["data"]))
     return D
+
+
+def csr_mv(op, shape, index_ptr, indices, data, x):
+    """CSR_mv (op 0), CSR_T_mv (op 1), CSR_mv_sym (op 2); returns (y, scale)."""
+    ptr = np.ascontiguousarray(index_ptr, dtype=np.int64)
+    idx = np.ascontiguousarray(indices, dtype=np.int64)
+    dat = np.ascontiguousarray(data, dtype=np.complex128)
+    xv = np.ascontiguousarray(x, dtype=np.complex128)
+    n_out = shape[1] if op == 1 else shape[0]
+    y = np.zeros(n_out, dtype=np.complex128)
+    sc = np.zeros(n_out)
+    lib().or_csr_mv(int(op), int(shape[0]), int(shape[1]), _p(ptr), _p(idx), _p(dat), _p(xv),
+                    _p(y), _p(sc))
+    return y, sc
+
+
+def csr_from_blocks(blocks, n_rb, n_cb):
+    """CSR_from_block of CSR dicts blocks[(i, j)]; returns one CSR dict."""
+    order = [blocks[(i, j)] for j in range(n_cb) for i in range(n_rb)]
+    nb = len(order)
+    shapes = np.array([b["shape"] for b in order], dtype=np.int64).reshape(nb, 2)
+    nnz = np.array([b["nnz"] for b in order], dtype=np.int64)
+    P, I, D = (ctypes.c_void_p * nb)(), (ctypes.c_void_p * nb)(), (ctypes.c_void_p * nb)()
+    keep = []
+    for k, b in enumerate(order):
+        if b["nnz"] > 0:
+            arrs = (np.ascontiguousarray(b["index_ptr"], dtype=np.int64),
+                    np.ascontiguousarray(b["indices"], dtype=np.int64),
+                    np.ascontiguousarray(b["data"], dtype=np.complex128))
+            keep.append(arrs)
+            P[k], I[k], D[k] = (a.ctypes.data for a in arrs)
+    rows = int(sum(shapes[i, 0] for i in range(n_rb)))
+    tot = int(nnz.sum())
+    out = dict(shape=(rows, int(sum(shapes[n_rb * j, 1] for j in range(n_cb)))), nnz=tot,
+               index_ptr=np.zeros(rows + 1, np.int64), indices=np.zeros(tot, np.int64),
+               data=np.zeros(tot, np.complex128))
+    n = lib().or_csr_from_blocks(n_rb, n_cb, _p(shapes), _p(nnz), P, I, D, _p(out["index_ptr"]),
+                                 _p(out["indices"]), _p(out["data"]))
+    assert n == tot
+    return out

@@ -6,6 +6,9 @@ wigner.json      exact 3j (a k b; 0 0 0) and 6j {la lb L; ld lc k} values from
                  general-m 3j symbols of the dipole factor (src/mat_els/dipole.f90:25).
 gauss_legendre.json  nodes/weights from numpy.polynomial.legendre.leggauss for
                  q = 1..24 (the reference's stdlib gauss_legendre, quad_tools.f90:26).
+ragged_problems.json the 64 radial problems of the ragged batch, drawn from
+                 numpy.random.default_rng(0) in the order: order k from {6,7,8},
+                 N in [100, 500], max_k in [4, 16], channel l_max in [0, 8].
 """
 import json
 import os
@@ -16,7 +19,22 @@ from sympy.physics.wigner import wigner_3j, wigner_6j
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
+def ragged():
+    rng = np.random.default_rng(0)
+    probs = []
+    for _ in range(64):
+        k = int(rng.choice([6, 7, 8]))
+        n = int(rng.integers(100, 501))
+        kmax = int(rng.integers(4, 17))
+        lmax = int(rng.integers(0, 9))
+        probs.append({"k": k, "n_b": n, "r_max": float(n), "k_GL": k + 4, "max_k": kmax,
+                      "l_max": lmax})
+    with open(os.path.join(HERE, "ragged_problems.json"), "w") as f:
+        json.dump(probs, f, indent=0)
+
+
 def main():
+    ragged()
     three = []
     for a in range(0, 11):
         for b in range(0, 11):

@@ -1,0 +1,104 @@
+"""Precision of the FP64 and mixed paths at the precision-study size: order 8,
+N=400 on the exp-linear grid to r_max=400, 10 Gauss-Legendre points per
+interval, multipoles k=0..12, l_max=6, singlet L=0..2 (natural parity).
+
+Against the FP64 CPU oracle:
+- every R^k element of the store, per k: max and RMS relative error of the
+  GPU FP64 store and of the mixed store (scaled FP32 pairs);
+- H and S entries of row samples of every block (oracle construct_block over
+  the same rows): pattern bit-exact, max and RMS error relative to the
+  entry's term magnitude.
+Takes several minutes (the oracle's primitives dominate), so it runs only
+with BS2E_PRECISION_REPORT=1; the JSON report goes to BS2E_REPORT_OUT.
+"""
+import json
+import os
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RUN = os.environ.get("BS2E_PRECISION_REPORT") == "1"
+WL = dict(k=8, n_b=400, r_max=400.0, q=10, max_k=12, lmax=6, max_L=2, Z=2)
+
+
+def _rel_stats(got, ref, scale):
+    r = np.abs(got - ref) / scale
+    return float(r.max()) if r.size else 0.0, float(np.sqrt(np.mean(r ** 2))) if r.size else 0.0
+
+
+@pytest.mark.skipif(not RUN, reason="set BS2E_PRECISION_REPORT=1 (runs for minutes)")
+def test_precision_report(bs2e, oracle):
+    w = WL
+    k, N, q, K1 = w["k"], w["n_b"], w["q"], w["max_k"] + 1
+    t = bs2e.grids.explin_knots(k, N, w["r_max"])
+    rep = {"workload": "order 8, N=400, r_max=400, q=10, k=0..12, l_max=6, singlet L=0..2",
+           "bars": {"fp64": 1e-12, "mixed": 1e-9}}
+    t0 = time.perf_counter()
+    prim = oracle.slater(t, k, q, w["max_k"])
+    R = oracle.rk_map(N, k, w["max_k"], prim)
+    rep["oracle_radial_s"] = time.perf_counter() - t0
+    H1p = oracle.setup_H1p(t, k, q, w["Z"], w["lmax"] + 1, cap_order=2, cap_r0=10.0,
+                           cap_eta=1e-3)
+    S = oracle.setup_S(t, k, q)
+    hd = bs2e.Bs2e(t, k, q, w["max_k"], precision=bs2e.PREC_FP64)
+    hm = bs2e.Bs2e(t, k, q, w["max_k"], precision=bs2e.PREC_MIXED)
+    for name, h in (("fp64", hd), ("mixed", hm)):
+        h.slater()
+        h.rk()  # warm
+        t0 = time.perf_counter()
+        h.slater()
+        h.rk()
+        rep["gpu_radial_s_" + name] = time.perf_counter() - t0
+        h.set_one_body(H1p, S)
+    per_k = []
+    for kk in range(K1):
+        ref = R[..., kk]
+        mask = ref != 0.0
+        vref = ref[mask]
+        assert (vref > 0).all()
+        row = {"k": kk, "elements": int(mask.sum())}
+        for name, h in (("fp64", hd), ("mixed", hm)):
+            g = h.rk_export(kk)[mask]
+            row[name + "_max"], row[name + "_rms"] = _rel_stats(g, vref, vref)
+        per_k.append(row)
+    rep["rk_per_k"] = per_k
+    blocks_rep = []
+    for L in range(w["max_L"] + 1):
+        cf = oracle.count_configs(L, L % 2, w["lmax"], N, k)
+        n = cf.size
+        for frac in (0.0, 0.37, 0.81):
+            r0 = int(frac * n)
+            r1 = min(n, r0 + 24)
+            Hr, Sr = oracle.construct_block(cf, L, k, N, w["max_k"], R, H1p, S, True, 0,
+                                            rows=(r0, r1))
+            ent = {"L": L, "rows": [r0, r1], "n_config": int(n), "nnz_H": int(Hr["nnz"]),
+                   "nnz_S": int(Sr["nnz"])}
+            for name, h in (("fp64", hd), ("mixed", hm)):
+                H, Sg = h.block_rows(cf, L, r0, r1 - r0, True, 0)
+                np.testing.assert_array_equal(H["index_ptr"], Hr["index_ptr"])
+                np.testing.assert_array_equal(H["indices"], Hr["indices"])
+                np.testing.assert_array_equal(Sg["indices"], Sr["indices"])
+                ent["H_" + name + "_max"], ent["H_" + name + "_rms"] = _rel_stats(
+                    H["data"], Hr["data"], np.maximum(Hr["scale"], 1e-300))
+                ent["S_" + name + "_max"], _ = _rel_stats(
+                    Sg["data"], Sr["data"], np.maximum(np.abs(Sr["data"]), 1e-300))
+            blocks_rep.append(ent)
+    rep["H_rows"] = blocks_rep
+    hd.close()
+    hm.close()
+    rep["summary"] = {
+        "rk_fp64_max": max(r["fp64_max"] for r in per_k),
+        "rk_mixed_max": max(r["mixed_max"] for r in per_k),
+        "H_fp64_max": max(e["H_fp64_max"] for e in blocks_rep),
+        "H_mixed_max": max(e["H_mixed_max"] for e in blocks_rep),
+    }
+    out = os.environ.get("BS2E_REPORT_OUT")
+    if out:
+        with open(out, "w") as f:
+            json.dump(rep, f, indent=1)
+    s = rep["summary"]
+    assert s["rk_fp64_max"] <= 1e-12 and s["H_fp64_max"] <= 1e-12
+    assert s["rk_mixed_max"] <= 1e-9 and s["H_mixed_max"] <= 1e-9
