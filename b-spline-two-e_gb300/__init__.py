@@ -394,6 +394,16 @@ class Bs2e:
         _check(self._h, lib().bs2e_set_radial_dipole(self._h, int(gauge), _ptr(r_mat),
                                                      _ptr(dr_mat), _ptr(r_inv_mat)))
 
+    def dip_block_count(self, rows, sym1, cols, sym2, q, compute=True):
+        """Non-zeros of a dipole block (count pass only)."""
+        rows, cols = as_configs(rows), as_configs(cols)
+        n = ctypes.c_int64()
+        _check(self._h, lib().bs2e_dip_block_count(self._h, _ptr(rows), rows.size,
+                                                   *[int(x) for x in sym1], _ptr(cols), cols.size,
+                                                   *[int(x) for x in sym2], int(q),
+                                                   int(bool(compute)), ctypes.byref(n)))
+        return n.value
+
     def dip_block(self, rows, sym1, cols, sym2, q, compute=True):
         """Dipole block between symmetries sym1 = (L1, M1, parity1) (rows) and
         sym2 = (L2, M2, parity2) (columns); returns a dict of 1-based CSR arrays."""

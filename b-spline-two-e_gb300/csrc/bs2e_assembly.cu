@@ -812,9 +812,10 @@ static inline unsigned grid_rows(int64_t n) {
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-void launch_cfg_equal(bs2e_handle *h, int64_t n) {
+void launch_cfg_equal(bs2e_handle *h, const bs2e_config *a, const bs2e_config *b, int64_t n,
+                      unsigned long long *stats) {
     if (n <= 0) return;
-    k_cfg_equal<<<grid_rows(n), 256, 0, h->stream>>>(h->blk.cfg_new, h->blk.cfg, n, h->blk.stats);
+    k_cfg_equal<<<grid_rows(n), 256, 0, h->stream>>>(a, b, n, stats);
     h->launches++;
 }
 

@@ -38,6 +38,7 @@ struct bs2e_batch {
     int threads[4] = {128, 256, 256, 256};
     int grid[4] = {1, 1, 1, 1};
     int chunk = 1;
+    int persistent = 1;  // R^k stage: queue-draining CTAs (1) or one CTA per chunk (0)
     int sms = 0;
     bool tuned = false;
     cudaGraph_t graph = nullptr;
@@ -78,42 +79,51 @@ bs2e_status bfail(bs2e_batch *b, bs2e_status st, const std::string &m) {
 // Persistent grid of a stage: every CTA the SMs hold at once (no more than
 // there are items).  Also sets the kernel's shared-memory limit, so it is
 // called outside graph capture.
-void set_grid(bs2e_batch *b, int stage) {
+void set_grid(bs2e_batch *b, int stage, int chunk = 1, int persistent = 1) {
     int per = radial_batch_blocks_per_sm(stage, b->threads[stage], b->smem[stage]);
     if (per < 1) per = 1;
     int64_t items = b->off[stage].back();
+    if (!persistent) {
+        b->grid[stage] = (int)std::max<int64_t>((items + chunk - 1) / chunk, 1);
+        return;
+    }
     b->grid[stage] = (int)std::min<int64_t>((int64_t)per * b->sms, std::max<int64_t>(items, 1));
 }
 
-void enqueue_stage(bs2e_batch *b, int stage, int chunk) {
+void enqueue_stage(bs2e_batch *b, int stage, int chunk, int persistent = 1) {
     const int n = (int)b->hs.size();
     launch_radial_batch(b->stream, stage, b->grid[stage], b->threads[stage], b->smem[stage],
                         b->d_probs, b->d_off + (size_t)stage * (n + 1), n, b->d_counter + stage,
-                        stage == 3 ? chunk : 1);
+                        stage == 3 ? chunk : 1, stage == 3 ? persistent : 1);
     b->launches++;
 }
 
 void enqueue_all(bs2e_batch *b) {
     cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(unsigned long long), b->stream);
-    for (int st = 0; st < 4; ++st) enqueue_stage(b, st, b->chunk);
+    for (int st = 0; st < 4; ++st) enqueue_stage(b, st, b->chunk, b->persistent);
 }
 
-// Times the R^k stage for each candidate shape and keeps the fastest.
+// Times the R^k stage for each candidate (threads per CTA x work
+// distribution: a queue drained by resident CTAs taking 1, 2 or 8 tiles per
+// access, or one CTA per 1 or 4 tiles) and keeps the fastest.
 bs2e_status tune(bs2e_batch *b) {
+    struct Cand {
+        int persistent, chunk;
+    };
     const int cand_threads[3] = {128, 256, 512};
-    const int cand_chunk[3] = {1, 2, 8};
+    const Cand cand[5] = {{1, 1}, {1, 2}, {1, 8}, {0, 1}, {0, 4}};
     cudaEvent_t e0, e1;
     BCU(cudaEventCreate(&e0));
     BCU(cudaEventCreate(&e1));
     float best = 1e30f;
-    int bt = 256, bc = 1;
+    int bt = 256, bc = 1, bp = 1;
     for (int t : cand_threads)
-        for (int c : cand_chunk) {
+        for (const Cand &c : cand) {
             b->threads[3] = t;
-            set_grid(b, 3);
+            set_grid(b, 3, c.chunk, c.persistent);
             BCU(cudaMemsetAsync(b->d_counter + 3, 0, sizeof(unsigned long long), b->stream));
             BCU(cudaEventRecord(e0, b->stream));
-            enqueue_stage(b, 3, c);
+            enqueue_stage(b, 3, c.chunk, c.persistent);
             BCU(cudaEventRecord(e1, b->stream));
             BCU(cudaEventSynchronize(e1));
             BCU(cudaGetLastError());
@@ -122,14 +132,16 @@ bs2e_status tune(bs2e_batch *b) {
             if (ms < best) {
                 best = ms;
                 bt = t;
-                bc = c;
+                bc = c.chunk;
+                bp = c.persistent;
             }
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     b->threads[3] = bt;
     b->chunk = bc;
-    set_grid(b, 3);
+    b->persistent = bp;
+    set_grid(b, 3, bc, bp);
     b->tuned = true;
     return BS2E_OK;
 }
@@ -182,13 +194,14 @@ BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, b
             for (bs2e_handle *h : b->hs) {
                 BCU(cudaStreamSynchronize(h->stream));
                 const Radial &g = h->g;
-                if (h->precision == BS2E_PREC_MIXED) {
+                const bool mixed = h->precision == BS2E_PREC_MIXED;
+                if (mixed) {
                     if (!h->d_Rf) BCU(cudaMalloc(&h->d_Rf, sizeof(float2) * (size_t)g.N * g.N * g.tile));
                     if (!h->d_Rexp) BCU(cudaMalloc(&h->d_Rexp, sizeof(int) * (size_t)g.N * g.N * g.K1));
-                    b->smem[3] = std::max(b->smem[3], (size_t)g.K1 * g.W * g.W * sizeof(double));
                 } else if (!h->d_R) {
                     BCU(cudaMalloc(&h->d_R, sizeof(double) * (size_t)g.N * g.N * g.tile));
                 }
+                b->smem[3] = std::max(b->smem[3], rk_store_smem(g, mixed));
                 b->smem[1] = std::max(b->smem[1], moments_smem(g));
                 probs.push_back(radial_dev(h));
                 const int64_t items[4] = {g.n_iv, (int64_t)g.n_iv * g.K1,
@@ -255,7 +268,7 @@ BS2E_API bs2e_status bs2e_batch_tuning(const bs2e_batch *b, int64_t *rk_threads,
                                        int64_t *graph_ready, int64_t *launches) {
     if (!b) return BS2E_ERR_ARG;
     if (rk_threads) *rk_threads = b->threads[3];
-    if (chunk) *chunk = b->chunk;
+    if (chunk) *chunk = b->persistent ? b->chunk : -b->chunk;
     if (graph_ready) *graph_ready = b->exec ? 1 : 0;
     if (launches) *launches = b->launches;
     return BS2E_OK;

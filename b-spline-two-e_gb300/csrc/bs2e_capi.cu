@@ -112,6 +112,10 @@ cudaError_t grow(T **p, int64_t &cap, int64_t n) {
         if (s_ != BS2E_OK) return s_;       \
     } while (0)
 
+// Device pointers from the caller: int64 arrays need 8-byte, complex128
+// arrays 16-byte alignment (the kernels use 16-byte vector accesses).
+inline bool aligned(const void *p, size_t a) { return ((uintptr_t)p % a) == 0; }
+
 // Uploads the configuration list and, unless it is the block counted last,
 // plans it on the device (channels, segment tables, order checks) and counts
 // its non-zeros with both the construct and the count_nnz predicates.
@@ -121,25 +125,68 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
     if (L < 0 || (spin != 0 && spin != 1) || (full != 0 && full != 1))
         return fail(h, BS2E_ERR_ARG, "L, spin or full out of range");
     if (n_config > ((int64_t)1 << 31) - 2) return fail(h, BS2E_ERR_ARG, "n_config too large");
-    DevBlock &B = h->blk;
     const Radial &g = h->g;
+    {
+        DevBlock &C = h->blk;
+        if (!C.stats) CU(dalloc(&C.stats, 8));
+        CU(grow(&C.cfg_new, C.cfg_new_cap, n_config));
+        if (n_config > 0)
+            CU(cudaMemcpyAsync(C.cfg_new, cf, sizeof(bs2e_config) * n_config,
+                               cudaMemcpyHostToDevice, h->stream));
+    }
+    unsigned long long st[8];
+    // is X the uploaded list?  (identity, then a device compare of every record)
+    auto same = [&](const DevBlock &X, bool &eq) -> bs2e_status {
+        eq = false;
+        if (!(X.valid && X.L == L && X.spin == spin && X.full == full && X.n == n_config))
+            return BS2E_OK;
+        DevBlock &C = h->blk;
+        CU(cudaMemsetAsync(C.stats, 0, 8 * sizeof(unsigned long long), h->stream));
+        launch_cfg_equal(h, C.cfg_new, X.cfg, n_config, C.stats);
+        CU(cudaMemcpyAsync(st, C.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
+        TRY(sync_check(h, "block compare"));
+        eq = st[6] == 0;
+        return BS2E_OK;
+    };
+    bool eq = false;
+    TRY(same(h->blk, eq));
+    if (eq) return BS2E_OK;  // the block counted last
+    for (size_t i = 0; i < h->parked.size(); ++i) {
+        TRY(same(h->parked[i].first, eq));
+        if (!eq) continue;
+        // a block counted earlier: make it current, park the current one first
+        auto e = std::move(h->parked[i]);
+        h->parked.erase(h->parked.begin() + (ptrdiff_t)i);
+        if (h->blk.valid) h->parked.insert(h->parked.begin(), {h->blk, h->plan});
+        else free_block(h->blk);
+        h->blk = e.first;
+        h->plan = e.second;
+        return BS2E_OK;
+    }
+    if (h->blk.valid) {
+        // park the current block; the upload moves to a fresh one
+        DevBlock nb;
+        std::swap(nb.cfg_new, h->blk.cfg_new);
+        std::swap(nb.cfg_new_cap, h->blk.cfg_new_cap);
+        h->parked.insert(h->parked.begin(), {h->blk, h->plan});
+        h->blk = nb;
+        int64_t rows = 0;
+        size_t keep = 0;
+        for (; keep < h->parked.size(); ++keep) {
+            rows += h->parked[keep].first.n;
+            if (keep >= (size_t)kBlockCache || rows > kBlockCacheRows) break;
+        }
+        while (h->parked.size() > keep) {
+            free_block(h->parked.back().first);
+            h->parked.pop_back();
+        }
+    }
+    DevBlock &B = h->blk;
     if (!B.stats) CU(dalloc(&B.stats, 8));
     if (!B.marks) CU(dalloc(&B.marks, kMaxCh + 1));
     if (!B.lmap) CU(dalloc(&B.lmap, (size_t)kMaxL * kMaxL));
     if (!B.chl) CU(dalloc(&B.chl, kMaxCh));
-    CU(grow(&B.cfg_new, B.cfg_new_cap, n_config));
-    if (n_config > 0)
-        CU(cudaMemcpyAsync(B.cfg_new, cf, sizeof(bs2e_config) * n_config, cudaMemcpyHostToDevice,
-                           h->stream));
     CU(cudaMemsetAsync(B.stats, 0, 8 * sizeof(unsigned long long), h->stream));
-    unsigned long long st[8];
-    if (B.valid && B.L == L && B.spin == spin && B.full == full && B.n == n_config) {
-        launch_cfg_equal(h, n_config);
-        CU(cudaMemcpyAsync(st, B.stats, sizeof(st), cudaMemcpyDeviceToHost, h->stream));
-        TRY(sync_check(h, "block compare"));
-        if (st[6] == 0) return BS2E_OK;  // same block as the last count
-        CU(cudaMemsetAsync(B.stats, 0, 8 * sizeof(unsigned long long), h->stream));
-    }
     B.valid = false;
     BlockPlan &P = h->plan;
     P = BlockPlan();
@@ -516,6 +563,8 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         cudaSetDevice(h->device);
         if (h->stream) cudaStreamSynchronize(h->stream);
         free_block(h->blk);
+        for (auto &e : h->parked) free_block(e.first);
+        h->parked.clear();
         dfree(h->d_knots);
         dfree(h->d_glx);
         dfree(h->d_glw);
@@ -721,6 +770,7 @@ BS2E_API bs2e_status bs2e_rk_export(bs2e_handle *h, int64_t k, double *out, int6
     if (!h->rk_done[k]) return fail(h, BS2E_ERR_STATE, "rk_export: multipole not built by bs2e_rk");
     const size_t n = (size_t)g.N * g.N * g.W * g.W;
     double *d = out;
+    if (on_device && !aligned(out, 8)) return fail(h, BS2E_ERR_ARG, "rk_export: out needs 8-byte alignment");
     if (!on_device) CU(dalloc(&d, n));
     launch_rk_slice(h, (int)k, d);
     bs2e_status st = BS2E_OK;
@@ -1013,6 +1063,9 @@ BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *confi
     if (!out_on_device)
         return stream_fill(h, configs, 0, n_config, H_index_ptr, H_indices, H_data, S_index_ptr,
                            S_indices, S_data);
+    if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
+        !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16))
+        return fail(h, BS2E_ERR_ARG, "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
     launch_block_scan(h, H_index_ptr, S_index_ptr, 0, n_config);
     FillRange r;
     r.row0 = 0;
@@ -1065,6 +1118,9 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
     if (!out_on_device)
         return stream_fill(h, configs, row_first, row_count, H_index_ptr, H_indices, H_data,
                            S_index_ptr, S_indices, S_data);
+    if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
+        !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16))
+        return fail(h, BS2E_ERR_ARG, "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
     launch_block_scan(h, H_index_ptr, S_index_ptr, row_first, row_count);
     FillRange r;
     r.row0 = row_first;
@@ -1180,6 +1236,8 @@ BS2E_API bs2e_status bs2e_dip_block_fill(bs2e_handle *h, const bs2e_config *rows
     TRY(dip_prepare(h, rows, n_rows, L1, M1, pi1, cols, n_cols, L2, M2, pi2, q, compute, D, empty,
                     nnz));
     const bool dev = out_on_device != 0;
+    if (dev && (!aligned(index_ptr, 8) || !aligned(indices, 8) || !aligned(data, 16)))
+        return fail(h, BS2E_ERR_ARG, "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
     if (empty) {
         std::vector<int64_t> ones((size_t)n_rows + 1, 1);
         if (dev)
@@ -1259,6 +1317,9 @@ BS2E_API bs2e_status bs2e_csr_mv(bs2e_handle *h, int64_t op, int64_t n_rows, int
     const int64_t *dp = index_ptr, *di = indices;
     const double2 *dA = (const double2 *)data, *dx = (const double2 *)x;
     double2 *dy = (double2 *)y;
+    if (on_device && (!aligned(index_ptr, 8) || !aligned(indices, 8) || !aligned(data, 16) ||
+                      !aligned(x, 16) || !aligned(y, 16)))
+        return fail(h, BS2E_ERR_ARG, "csr_mv: int64 arrays need 8-byte, complex arrays 16-byte alignment");
     if (!on_device) {
         if (index_ptr[n_rows] - 1 != nnz)
             return fail(h, BS2E_ERR_ARG, "csr_mv: index_ptr(n_rows+1) - 1 differs from nnz");
@@ -1328,6 +1389,8 @@ BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t 
     }
     const int64_t n_rows = row0[n_rb];
     if (tot > 0 && (!out_indices || !out_data)) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: NULL output");
+    if (on_device && (!aligned(out_index_ptr, 8) || !aligned(out_indices, 8) || !aligned(out_data, 16)))
+        return fail(h, BS2E_ERR_ARG, "csr_from_blocks: int64 arrays need 8-byte, data 16-byte alignment");
     if (n_rows == 0) {
         if (tot > 0) return fail(h, BS2E_ERR_ARG, "csr_from_blocks: entries in blocks without rows");
         const int64_t one = 1;
@@ -1358,6 +1421,10 @@ BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t 
             col += shapes[2 * b + 1];
             if (nnz[b] <= 0) continue;
             if (on_device) {
+                if (!aligned(index_ptr[b], 8) || !aligned(indices[b], 8) || !aligned(data[b], 16)) {
+                    cleanup();
+                    return fail(h, BS2E_ERR_ARG, "csr_from_blocks: int64 arrays need 8-byte, data 16-byte alignment");
+                }
                 B.ptr = index_ptr[b];
                 B.idx = indices[b];
                 B.data = (const double2 *)data[b];
@@ -1365,7 +1432,9 @@ BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t 
             }
             const int64_t rows = shapes[2 * b];
             char *d = nullptr;
-            const size_t bytes = 8 * (size_t)(rows + 1) + 8 * (size_t)nnz[b] + 16 * (size_t)nnz[b];
+            // complex data 16-byte aligned after the int64 pointers and columns
+            const size_t o_dat = (8 * (size_t)(rows + 1 + nnz[b]) + 15) / 16 * 16;
+            const size_t bytes = o_dat + 16 * (size_t)nnz[b];
             cudaError_t e = cudaMalloc(&d, bytes);
             if (e != cudaSuccess) {
                 cleanup();
@@ -1373,7 +1442,7 @@ BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t 
             }
             staged.push_back(d);
             int64_t *dp = (int64_t *)d, *di = dp + rows + 1;
-            double2 *dd = (double2 *)(di + nnz[b]);
+            double2 *dd = (double2 *)(d + o_dat);
             e = cudaMemcpyAsync(dp, index_ptr[b], 8 * (size_t)(rows + 1), cudaMemcpyHostToDevice, h->stream);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(di, indices[b], 8 * (size_t)nnz[b], cudaMemcpyHostToDevice, h->stream);

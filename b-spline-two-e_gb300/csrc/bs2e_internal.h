@@ -41,6 +41,9 @@ struct PairInfo {
 
 constexpr int kMaxL = 64;    // l1, l2 < 64 (channel lookup table is kMaxL x kMaxL)
 constexpr int kMaxCh = 256;  // channels per symmetry block
+// counted blocks kept besides the current one (and their total rows)
+constexpr int kBlockCache = 16;
+constexpr int64_t kBlockCacheRows = (int64_t)1 << 26;
 
 // Host-side plan of one symmetry block: its channels (in configuration
 // order) and the angular coupling of every (row channel, column channel).
@@ -137,9 +140,11 @@ struct bs2e_handle {
     bool have_one_body = false;
     bool s_real = true;
     bool ff_one_body = false;  // mixed path may use the FP32-pair bands
-    // block cache
+    // the block counted last (plan + device state) and up to kBlockCache
+    // earlier ones, most recently used first
     bs2e::BlockPlan plan;
     bs2e::DevBlock blk;
+    std::vector<std::pair<bs2e::DevBlock, bs2e::BlockPlan>> parked;
     // radial dipole bands (M1, M2) and dipole-block work buffers
     double2 *d_dM1 = nullptr, *d_dM2 = nullptr;
     int dip_gauge = -1;
@@ -196,8 +201,9 @@ RadialDev radial_dev(const bs2e_handle *h);
 int radial_batch_blocks_per_sm(int stage, int threads, size_t smem);
 void launch_radial_batch(cudaStream_t s, int stage, int grid, int threads, size_t smem,
                          const RadialDev *probs, const int64_t *off, int n,
-                         unsigned long long *counter, int chunk);
+                         unsigned long long *counter, int chunk, int persistent);
 size_t moments_smem(const Radial &g);
+size_t rk_store_smem(const Radial &g, bool mixed);
 void launch_tabulate(bs2e_handle *h);
 void launch_moments(bs2e_handle *h);
 void launch_totals(bs2e_handle *h);
@@ -233,7 +239,8 @@ void launch_dip_count(bs2e_handle *h, const DipDev &D, int64_t *cnt);
 void launch_dip_fill(bs2e_handle *h, const DipDev &D, const int64_t *ptr, int64_t *idx,
                      double2 *dat);
 // Kernel launchers (bs2e_assembly.cu)
-void launch_cfg_equal(bs2e_handle *h, int64_t n);
+void launch_cfg_equal(bs2e_handle *h, const bs2e_config *a, const bs2e_config *b, int64_t n,
+                      unsigned long long *stats);
 void launch_chan_marks(bs2e_handle *h, int64_t n);
 void launch_plan_seg(bs2e_handle *h, int64_t n);
 void launch_block_count(bs2e_handle *h);

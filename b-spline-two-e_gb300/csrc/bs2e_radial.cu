@@ -267,36 +267,116 @@ __device__ __forceinline__ double rk_element(const double *__restrict__ mom,
     return v;
 }
 
-// Tile t = a * N + b of the FP64 store (block-wide).
-__device__ void rk_tile_fp64(const RadialDev &P, int64_t t, int k_first, int k_count) {
+// Near-field tiles (|a - b| < k, where the interval ranges of an (a, c) pair
+// and a (b, d) pair can meet).  With iv2_j = b - k + 2 + j (j < k) the
+// intervals a (b, d) pair can use, the two triangles of the interval-pair
+// sum factor through prefix sums over the (a, c) intervals,
+//   Pm[j] = sum_{iv1 < iv2_j} m(ac, iv1),    SM[j] = sum_{iv1 > iv2_j} M(ac, iv1),
+//   R = sum_j ( M(bd, iv2_j) Pm[j] + m(bd, iv2_j) SM[j] )
+//       + sum_{shared iv} D(iv; ac, bd) + D(iv; bd, ac),
+// 2k FMAs per element instead of up to k^2 products.  Both sums add
+// positive moments (B-splines are non-negative), so the regrouping keeps full
+// accuracy.  Staged per multipole in s[4][k][W]: Pm, SM over dc; m, M over dd.
+__device__ void rk_near_stage(const RadialDev &P, int a, int b, int kk, double *s) {
+    const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
+    const int base2 = b - k + 2;
+    const double *__restrict__ mom = P.mom;
+    for (int x = threadIdx.x; x < 2 * W * k; x += blockDim.x) {
+        const bool ac = x < W * k;
+        const int y = ac ? x : x - W * k;
+        const int off = y / k, j = y - off * k;
+        const int iv2 = base2 + j;
+        double v0 = 0.0, v1 = 0.0;
+        if (ac) {
+            const int c = a + off - (k - 1);
+            if (c >= 0 && c < N) {
+                const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
+                for (int iv1 = lop; iv1 <= min(hip, iv2 - 1); ++iv1)
+                    v0 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+                for (int iv1 = max(lop, iv2 + 1); iv1 <= hip; ++iv1)
+                    v1 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+            }
+            s[j * W + off] = v0;          // Pm
+            s[(k + j) * W + off] = v1;    // SM
+        } else {
+            const int d = b + off - (k - 1);
+            if (d >= 0 && d < N) {
+                const int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
+                if (iv2 >= loq && iv2 <= hiq) {
+                    const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
+                    const int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
+                    v0 = m2[pb];
+                    v1 = m2[k2 + pb];
+                }
+            }
+            s[(2 * k + j) * W + off] = v0;  // m(bd)
+            s[(3 * k + j) * W + off] = v1;  // M(bd)
+        }
+    }
+}
+
+__device__ __forceinline__ double rk_near_element(const RadialDev &P, const double *s, int a,
+                                                  int b, int kk, int dc, int dd) {
+    const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
+    const int c = a + dc - (k - 1), d = b + dd - (k - 1);
+    if (c < 0 || c >= N || d < 0 || d >= N) return 0.0;
+    double v = 0.0;
+    for (int j = 0; j < k; ++j) {
+        v = fma(s[(3 * k + j) * W + dd], s[j * W + dc], v);
+        v = fma(s[(2 * k + j) * W + dd], s[(k + j) * W + dc], v);
+    }
+    const int lo = max(max(max(a, c), max(b, d)) - k + 2, 0);
+    const int hi = min(min(min(a, c), min(b, d)) + 1, n_iv - 1);
+    for (int iv = lo; iv <= hi; ++iv) {
+        const int pa = (a + 1 - iv) * k + (c + 1 - iv), pb = (b + 1 - iv) * k + (d + 1 - iv);
+        const double *D = P.dint + ((size_t)iv * K1 + kk) * (size_t)k2 * k2;
+        v += D[(size_t)pa * k2 + pb] + D[(size_t)pb * k2 + pa];
+    }
+    return v;
+}
+
+__host__ __device__ __forceinline__ size_t rk_near_scratch(int k) {
+    return (size_t)4 * k * (2 * k - 1);  // doubles
+}
+
+// Values of multipoles [k_first, k_first + k_count) of tile t = a * N + b:
+// out[kk * W^2 + dc * W + dd] (block-wide; s: rk_near_scratch doubles).
+__device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k_count,
+                               double *out, double *s) {
     const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
     const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
-    double *dst = P.R + (size_t)t * P.tile;
-    const int nel = K1 * W2;
-    for (int e = threadIdx.x; e < P.tile; e += blockDim.x) {
-        if (e >= nel) {
-            dst[e] = 0.0;
-            continue;
+    if (abs(a - b) >= k) {  // far field everywhere: products of pair totals
+        for (int e = threadIdx.x; e < k_count * W2; e += blockDim.x) {
+            const int kk = k_first + e / W2, r = e % W2;
+            out[kk * W2 + r] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk,
+                                          r / W, r % W);
         }
-        int kk = e / W2, rem = e - kk * W2;
-        if (kk < k_first || kk >= k_first + k_count) continue;
-        int dc = rem / W, dd = rem - dc * W;
-        dst[e] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk, dc, dd);
+        return;
     }
+    for (int kk = k_first; kk < k_first + k_count; ++kk) {
+        __syncthreads();
+        rk_near_stage(P, a, b, kk, s);
+        __syncthreads();
+        for (int r = threadIdx.x; r < W2; r += blockDim.x)
+            out[kk * W2 + r] = rk_near_element(P, s, a, b, kk, r / W, r % W);
+    }
+}
+
+// Tile t = a * N + b of the FP64 store (block-wide).
+__device__ void rk_tile_fp64(const RadialDev &P, int64_t t, int k_first, int k_count, double *s) {
+    const int k = P.k, K1 = P.K1, W = 2 * k - 1;
+    double *dst = P.R + (size_t)t * P.tile;
+    const int nel = K1 * W * W;
+    for (int e = nel + threadIdx.x; e < P.tile; e += blockDim.x) dst[e] = 0.0;
+    rk_tile_values(P, t, k_first, k_count, dst, s);
 }
 
 // Tile t of the mixed store (block-wide); sv holds K1 W^2 doubles.
 __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_count,
-                              double *sv, int *sexp) {
-    const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
-    const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
+                              double *sv, int *sexp, double *s) {
+    const int k = P.k, K1 = P.K1, W = 2 * k - 1, W2 = W * W;
     const int nel = K1 * W2;
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-        int kk = e / W2, rem = e - kk * W2;
-        if (kk < k_first || kk >= k_first + k_count) continue;
-        int dc = rem / W, dd = rem - dc * W;
-        sv[e] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk, dc, dd);
-    }
+    rk_tile_values(P, t, k_first, k_count, sv, s);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int kk = k_first + warp; kk < k_first + k_count; kk += nwarp) {
@@ -327,13 +407,15 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
 }
 
 __global__ void k_rk_store(RadialDev P, int k_first, int k_count) {
-    rk_tile_fp64(P, blockIdx.x, k_first, k_count);
+    extern __shared__ double scr[];  // rk_near_scratch(k) doubles
+    rk_tile_fp64(P, blockIdx.x, k_first, k_count, scr);
 }
 
 __global__ void k_rk_store_mixed(RadialDev P, int k_first, int k_count) {
-    extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile
+    extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile, then the scratch
     __shared__ int sexp[kMaxK1];
-    rk_tile_mixed(P, blockIdx.x, k_first, k_count, sv, sexp);
+    rk_tile_mixed(P, blockIdx.x, k_first, k_count, sv, sexp,
+                  sv + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
 }
 
 // ---------------------------------------------------------------------------
@@ -347,6 +429,7 @@ struct BatchStage {
     const RadialDev *probs;
     const int64_t *off;  // [n + 1]
     int n, chunk;
+    int persistent;  // 1: CTAs drain the queue; 0: CTA x takes items [x chunk, (x + 1) chunk)
     unsigned long long *counter;
 };
 
@@ -368,8 +451,12 @@ __global__ void k_radial_batch(BatchStage B) {
     __shared__ int sexp[kMaxK1];
     __shared__ unsigned long long s_it;
     const int64_t total = B.off[B.n];
-    for (;;) {
-        if (threadIdx.x == 0) s_it = atomicAdd(B.counter, (unsigned long long)B.chunk);
+    for (int pass = 0;; ++pass) {
+        if (B.persistent) {
+            if (threadIdx.x == 0) s_it = atomicAdd(B.counter, (unsigned long long)B.chunk);
+        } else if (threadIdx.x == 0) {
+            s_it = pass == 0 ? (unsigned long long)blockIdx.x * B.chunk : (unsigned long long)total;
+        }
         __syncthreads();
         const int64_t it0 = (int64_t)s_it;
         __syncthreads();
@@ -389,9 +476,10 @@ __global__ void k_radial_batch(BatchStage B) {
                 if (e < totals_count(P)) totals_elem(P, e);
             } else {
                 if (P.mixed)
-                    rk_tile_mixed(P, li, 0, P.K1, sm, sexp);
+                    rk_tile_mixed(P, li, 0, P.K1, sm, sexp,
+                                  sm + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
                 else
-                    rk_tile_fp64(P, li, 0, P.K1);
+                    rk_tile_fp64(P, li, 0, P.K1, sm);
                 __syncthreads();
             }
         }
@@ -589,15 +677,21 @@ void launch_totals(bs2e_handle *h) {
     h->launches++;
 }
 
+size_t rk_store_smem(const Radial &g, bool mixed) {
+    return sizeof(double) * (rk_near_scratch(g.k) + (mixed ? (size_t)g.K1 * g.W * g.W : 0));
+}
+
 void launch_rk_fill(bs2e_handle *h, int k_first, int k_count) {
     const Radial &g = h->g;
     unsigned tiles = (unsigned)((int64_t)g.N * g.N);
-    if (h->precision == BS2E_PREC_MIXED) {
-        size_t smem = (size_t)g.K1 * g.W * g.W * sizeof(double);
+    const bool mixed = h->precision == BS2E_PREC_MIXED;
+    const size_t smem = rk_store_smem(g, mixed);
+    if (mixed) {
         cudaFuncSetAttribute(k_rk_store_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_rk_store_mixed<<<tiles, 256, smem, h->stream>>>(radial_dev(h), k_first, k_count);
     } else {
-        k_rk_store<<<tiles, 256, 0, h->stream>>>(radial_dev(h), k_first, k_count);
+        cudaFuncSetAttribute(k_rk_store, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_rk_store<<<tiles, 256, smem, h->stream>>>(radial_dev(h), k_first, k_count);
     }
     h->launches++;
 }
@@ -623,12 +717,13 @@ int radial_batch_blocks_per_sm(int stage, int threads, size_t smem) {
 
 void launch_radial_batch(cudaStream_t s, int stage, int grid, int threads, size_t smem,
                          const RadialDev *probs, const int64_t *off, int n,
-                         unsigned long long *counter, int chunk) {
+                         unsigned long long *counter, int chunk, int persistent) {
     BatchStage B;
     B.probs = probs;
     B.off = off;
     B.n = n;
     B.chunk = chunk;
+    B.persistent = persistent;
     B.counter = counter;
     switch (stage) {
         case 0: k_radial_batch<0><<<grid, threads, smem, s>>>(B); break;

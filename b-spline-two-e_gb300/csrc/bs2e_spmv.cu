@@ -20,11 +20,17 @@
 namespace bs2e {
 namespace {
 
+// acc += a x in complex FP64.  The imaginary part of most entries is zero
+// (the two-electron and overlap terms are real; only the CAP one-body term is
+// complex), so its two FMAs run only where it is not: the FP64 pipe, not
+// HBM, bounds this kernel otherwise.
 __device__ __forceinline__ void cmac(double &re, double &im, double2 a, double2 x) {
     re = fma(a.x, x.x, re);
-    re = fma(-a.y, x.y, re);
     im = fma(a.x, x.y, im);
-    im = fma(a.y, x.x, im);
+    if (a.y != 0.0) {
+        re = fma(-a.y, x.y, re);
+        im = fma(a.y, x.x, im);
+    }
 }
 
 // OP 0: y = A x.  OP 1: y += A^T x (y zeroed).  OP 2: y += U x + (U - diag)^T x

@@ -336,7 +336,9 @@ BS2E_API bs2e_status bs2e_csr_from_blocks(bs2e_handle *h, int64_t n_rb, int64_t 
 typedef struct bs2e_batch bs2e_batch;
 BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, bs2e_batch **out);
 BS2E_API bs2e_status bs2e_batch_run(bs2e_batch *b);
-/* The tuned R^k shape, whether the graph exists, and kernels launched so far. */
+/* The tuned R^k shape (threads per CTA; tiles per queue access, negative when
+ * each CTA takes a fixed chunk instead of draining the queue), whether the
+ * graph exists, and the kernels launched so far. */
 BS2E_API bs2e_status bs2e_batch_tuning(const bs2e_batch *b, int64_t *rk_threads, int64_t *chunk,
                                        int64_t *graph_ready, int64_t *launches);
 BS2E_API bs2e_status bs2e_batch_destroy(bs2e_batch *b);

@@ -187,3 +187,21 @@ def test_gpu_mv_empty_and_errors(bs2e):
         ok = dict(shape=(2, 2), nnz=2, index_ptr=np.array([1, 2, 3]), indices=np.array([2, 1]),
                   data=np.array([2.0, 3.0 + 1j]))
         np.testing.assert_allclose(h.csr_mv(ok, np.array([1.0, 1j])), [2j, 3 + 1j])
+
+
+@pytest.mark.gpu
+def test_misaligned_device_pointers_rejected(bs2e):
+    """Device pointers that break the 8/16-byte alignment of int64 / complex128
+    arrays are refused on the host before any kernel runs."""
+    torch = pytest.importorskip("torch")
+    c = CASES["cfg1"]
+    dev = torch.device("cuda", 0)
+    raw = torch.zeros(64, dtype=torch.float64, device=dev)
+    p = raw.data_ptr()
+    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+        with pytest.raises(bs2e.Bs2eError, match="align"):
+            h.csr_mv_device(0, 2, 2, 2, p, p + 24, p + 8 * 9, p + 8 * 20, p + 8 * 30)
+        # the handle stays usable
+        ok = dict(shape=(1, 1), nnz=1, index_ptr=np.array([1, 2]), indices=np.array([1]),
+                  data=np.array([2.0 + 0j]))
+        np.testing.assert_allclose(h.csr_mv(ok, np.array([3.0 + 0j])), [6.0])
