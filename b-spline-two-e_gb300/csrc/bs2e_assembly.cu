@@ -475,6 +475,371 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
 #define BS2E_FILL_MIN_BLOCKS 8
 #endif
 
+// Direct + exchange multipole sums of one entry in FP64 from the mixed store
+// (each stored pair rescaled exactly to its value), for channel pairs whose
+// slice maxima are too far apart for one FP32-pair frame.
+__device__ __forceinline__ double wide_sums(const float2 *R2, const int *sexp, const int8_t *kd,
+                                            const int8_t *kx, const double *ad, const double *ax,
+                                            int nd, int nx, int W2, bool sup, bool supx, int n_c,
+                                            int n_d, int n_a, int n_b, int k, int W) {
+    double rd = 0.0, rx = 0.0;
+    if (sup) {
+        const int od = (n_c - n_a + k - 1) * W + (n_d - n_b + k - 1);
+        for (int u = 0; u < nd; ++u) {
+            const int kk = kd[u];
+            const float2 p = R2[kk * W2 + od];
+            const double sc = __longlong_as_double((long long)(1023 - kRkBias + sexp[kk]) << 52);
+            rd = fma(((double)p.x + (double)p.y) * sc, ad[u], rd);
+        }
+    }
+    if (supx) {
+        const int ox = (n_d - n_a + k - 1) * W + (n_c - n_b + k - 1);
+        for (int u = 0; u < nx; ++u) {
+            const int kk = kx[u];
+            const float2 p = R2[kk * W2 + ox];
+            const double sc = __longlong_as_double((long long)(1023 - kRkBias + sexp[kk]) << 52);
+            rx = fma(((double)p.x + (double)p.y) * sc, ax[u], rx);
+        }
+    }
+    return (sup && supx) ? rd + rx : (sup ? rd : rx);
+}
+
+// One row of the block (warp-wide): row (n_a, n_b) of channel c_r, with the R^k
+// tile of (n_a, n_b) at sR (shared memory when staged, global otherwise), its
+// per-multipole exponents at sexp (mixed store) and the warp's scratch for the
+// scaled multipole weights.
+template <bool MIXED>
+__device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const int c_r,
+                                         const int n_a, const int n_b, const double *sR,
+                                         const int *sexp, float2 (*sAw)[kMaxK1],
+                                         int (*sKow)[kMaxK1]) {
+    const BlockArgs &A = F.B;
+    const float2 *sR2 = (const float2 *)sR;
+    const int k = A.k, W = 2 * k - 1, W2 = W * W, K1 = A.K1;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const int l_a = A.chl[c_r] >> 8, l_b = A.chl[c_r] & 255;  // row channel (l1, l2)
+    // FP32-pair band rows of this row: X_row[d] = X[n][n+d], |d| < k
+    const size_t ra = (size_t)(n_a - 1) * W + (k - 1), rb = (size_t)(n_b - 1) * W + (k - 1);
+    const float4 *HaA = F.Hbf ? F.Hbf + (size_t)l_a * A.N * W + ra : nullptr;  // H_la[n_a][.]
+    const float4 *HbB = F.Hbf ? F.Hbf + (size_t)l_b * A.N * W + rb : nullptr;  // H_lb[n_b][.]
+    const float4 *SA = F.Sbf ? F.Sbf + ra : nullptr;                           // S[n_a][.]
+    const float4 *SB = F.Sbf ? F.Sbf + rb : nullptr;                           // S[n_b][.]
+    int64_t oH = F.Hptr[row - F.ptr_row0] - 1 - F.Hbase;
+    int64_t oS = F.Sptr[row - F.ptr_row0] - 1 - F.Sbase;
+    for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
+        const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
+        const int flags = pi.flags;
+        const bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
+        const bool Aok = dir_ok || leq || leqx, Bok = ex_ok || leq || leqx;
+        if (!Aok && !Bok) continue;
+        const int nlo = (!A.full && c_c == c_r) ? n_a : 1;
+        const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, Aok, Bok, nlo);
+        const int ncand = cand.l1 + cand.l2;
+        const size_t pbase = ((size_t)c_r * A.n_ch + c_c) * 2 * K1;
+        const int8_t *kd = A.pair_k + pbase;
+        const int8_t *kx = kd + K1;
+        const double *ad = A.pair_a + pbase;
+        const double *ax = ad + K1;
+        int Ed = 0, Ex = 0;
+        bool wide = false;
+        if (MIXED) {
+            // scaled multipole weights of this channel pair for this tile
+            int ed = -100000, ex = -100000;
+            if (lane < pi.nd) ed = sexp[kd[lane]];
+            if (lane < pi.nx) ex = sexp[kx[lane]];
+            Ed = ed;
+            Ex = ex;
+            int md = lane < pi.nd ? ed : 100000, mx = lane < pi.nx ? ex : 100000;
+            for (int o = 16; o > 0; o >>= 1) {
+                Ed = max(Ed, __shfl_xor_sync(FULL, Ed, o));
+                Ex = max(Ex, __shfl_xor_sync(FULL, Ex, o));
+                md = min(md, __shfl_xor_sync(FULL, md, o));
+                mx = min(mx, __shfl_xor_sync(FULL, mx, o));
+            }
+            // slice maxima more than 2^120 apart: a weight rescaled to the
+            // largest would flush while the element of its slice may still
+            // matter for an entry, so this pair's sums run in FP64 instead
+            // (likewise the direct and exchange frames, which are joined)
+            wide = (pi.nd > 0 && Ed - md > 120) || (pi.nx > 0 && Ex - mx > 120) ||
+                   (pi.nd > 0 && pi.nx > 0 && abs(Ed - Ex) > 120);
+            if (lane < pi.nd) {
+                const float *af = A.pair_af + (pbase + lane) * 2;
+                float sc = pow2f(ed - Ed);
+                sAw[0][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
+                sKow[0][lane] = kd[lane] * W2;
+            }
+            if (lane < pi.nx) {
+                const float *af = A.pair_af + (pbase + K1 + lane) * 2;
+                float sc = pow2f(ex - Ex);
+                sAw[1][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
+                sKow[1][lane] = kx[lane] * W2;
+            }
+            __syncwarp();
+        }
+        for (int g0 = 0; g0 < ncand; g0 += 32) {
+            const int ci = g0 + lane;
+            Iv2 hs{0, 0, 0, 0}, ss{0, 0, 0, 0};
+            int base = 0, lo = 0, n_c = 0;
+            if (ci < ncand) {
+                n_c = iv2_at(cand, ci);
+                col_sets(A, c_r, c_c, n_a, n_b, n_c, flags, hs, ss, base, lo);
+            }
+            // H runs
+            {
+                int cnt = hs.l1 + hs.l2;
+                int incl = cnt;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                const int excl = incl - cnt;
+                const int tot = __shfl_sync(FULL, incl, 31);
+                for (int e0 = 0; e0 < tot; e0 += 32) {
+                    const int e = e0 + lane;
+                    int pos = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        int cand_pos = pos + step;
+                        int v = __shfl_sync(FULL, excl, cand_pos);
+                        if (v <= e) pos = cand_pos;
+                    }
+                    const int o_ex = __shfl_sync(FULL, excl, pos);
+                    const int r_nc = __shfl_sync(FULL, n_c, pos);
+                    const int r_base = __shfl_sync(FULL, base, pos);
+                    const int r_lo = __shfl_sync(FULL, lo, pos);
+                    const int r_s1 = __shfl_sync(FULL, hs.s1, pos);
+                    const int r_l1 = __shfl_sync(FULL, hs.l1, pos);
+                    const int r_s2 = __shfl_sync(FULL, hs.s2, pos);
+                    if (e < tot) {
+                        const int o = e - o_ex;
+                        const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
+                        const int j = r_base + (n_d - r_lo);
+                        const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
+                        const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
+                        double re = 0.0, im = 0.0;
+                        const bool r12 = (sup && dir_ok) || (supx && ex_ok);
+                        const bool one = (sup && leq) || (supx && leqx);
+                        if (MIXED && F.ff_one_body) {
+                            // everything in FP32-pair arithmetic, one rounding to double
+                            FF v{0.f, 0.f};
+                            int Ev = 0;
+                            bool has = false;
+                            double wide_re = 0.0;
+                            if (r12 && wide) {
+                                wide_re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2,
+                                                    sup, supx, r_nc, n_d, n_a, n_b, k, W);
+                            } else if (r12) {
+                                const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
+                                const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
+                                FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                if (sup)
+                                    for (int u = 0; u < pi.nd; ++u)
+                                        ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
+                                if (supx)
+                                    for (int u = 0; u < pi.nx; ++u)
+                                        ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
+                                v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
+                            }
+                            FF hi_im{0.f, 0.f};
+                            if (one) {
+                                // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
+                                // term is non-zero only under sup, the l_eq_ex term only
+                                // under sup_x, so both lookups stay inside the band
+                                FF hr{0.f, 0.f};
+                                if (leq && sup) {
+                                    const int dc = r_nc - n_a, dd = n_d - n_b;
+                                    float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                                    float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                    hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                ff_mul(make_float2(h2.x, h2.y), s2r));
+                                    hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                   ff_mul(make_float2(h2.z, h2.w), s2r));
+                                }
+                                if (leqx && supx) {
+                                    const int dc = n_d - n_a, dd = r_nc - n_b;
+                                    float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                                    float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                    bool ng = pi.sgn < 0.0;
+                                    FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                   ff_mul(make_float2(h2.x, h2.y), s2r));
+                                    FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                   ff_mul(make_float2(h2.z, h2.w), s2r));
+                                    hr = ff_add(hr, ff_neg_if(xr, ng));
+                                    hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
+                                }
+                                // the one-body part is in absolute scale (exponent
+                                // kRkBias in the pair's frame), the two-electron part
+                                // in its slice's frame Ev: joined as FP32 pairs while
+                                // the factor 2^(Ev - kRkBias) that rescales the latter
+                                // is a normal float with margin (slice maxima above
+                                // 2^-12, radii below ~4000 a.u., for kRkBias = 112),
+                                // in FP64 otherwise
+                                if (!has || kRkBias - Ev <= 124) {
+                                    v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
+                                    has = true;
+                                } else {
+                                    re = ff_to_double(hr, 0);
+                                }
+                            }
+                            if (has) re = re + ff_to_double(v, Ev - kRkBias);
+                            re = re + wide_re;
+                            im = one ? ff_to_double(hi_im, 0) : 0.0;
+                        } else if (r12) {
+                            const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
+                            const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
+                            if (MIXED && wide) {
+                                re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2, sup,
+                                               supx, r_nc, n_d, n_a, n_b, k, W);
+                            } else if (MIXED) {
+                                FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                if (sup)
+                                    for (int u = 0; u < pi.nd; ++u)
+                                        ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
+                                if (supx)
+                                    for (int u = 0; u < pi.nx; ++u)
+                                        ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
+                                int Ev;
+                                FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                re = ff_to_double(v, Ev - kRkBias);
+                            } else {
+                                // direct and exchange multipole sums; the add joining
+                                // them runs only where both are present
+                                double rd = 0.0, rx = 0.0;
+                                if (sup) {
+                                    const double *Rt = sR + od;
+                                    for (int u = 0; u < pi.nd; ++u) rd = fma(Rt[kd[u] * W2], ad[u], rd);
+                                }
+                                if (supx) {
+                                    const double *Rt = sR + ox;
+                                    for (int u = 0; u < pi.nx; ++u) rx = fma(Rt[kx[u] * W2], ax[u], rx);
+                                }
+                                re = (sup && supx) ? rd + rx : (sup ? rd : rx);
+                            }
+                        }
+                        if (one && !(MIXED && F.ff_one_body) && F.s_real) {
+                            // H_1p_neq (mat_els.f90:697-715) with a real S: the l_eq
+                            // term is non-zero only under sup, the l_eq_ex term only
+                            // under sup_x (both lookups inside the band)
+                            const int N = A.N;
+                            const double2 *Ha = F.Hb + (size_t)l_a * N * W;
+                            const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
+                            double hr = 0.0, hi = 0.0;
+                            if (leq && sup) {
+                                const double2 h1 = band(Ha, N, k, n_a, r_nc), h2 = band(Hbb, N, k, n_b, n_d);
+                                const double s1 = band(F.Sb, N, k, n_b, n_d).x, s2 = band(F.Sb, N, k, n_a, r_nc).x;
+                                hr = fma(h1.x, s1, h2.x * s2);
+                                hi = fma(h1.y, s1, h2.y * s2);
+                            }
+                            if (leqx && supx) {
+                                const double2 h1 = band(Ha, N, k, n_a, n_d), h2 = band(Hbb, N, k, n_b, r_nc);
+                                const double s1 = band(F.Sb, N, k, n_b, r_nc).x, s2 = band(F.Sb, N, k, n_a, n_d).x;
+                                hr = fma(pi.sgn, fma(h1.x, s1, h2.x * s2), hr);
+                                hi = fma(pi.sgn, fma(h1.y, s1, h2.y * s2), hi);
+                            }
+                            re = re + hr;
+                            im = im + hi;
+                        } else if (one && !(MIXED && F.ff_one_body)) {
+                            // H_1p_neq (mat_els.f90:697-715), complex S
+                            const int N = A.N;
+                            const double2 *Ha = F.Hb + (size_t)l_a * N * W;
+                            const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
+                            double2 h1 = make_double2(0.0, 0.0);
+                            if (leq) {
+                                double2 t1 = cmul(band(Ha, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d));
+                                double2 t2 = cmul(band(Hbb, N, k, n_b, n_d), band(F.Sb, N, k, n_a, r_nc));
+                                h1 = cadd(cadd(h1, t1), t2);
+                            }
+                            if (leqx) {
+                                double2 t1 = cmul(band(Ha, N, k, n_a, n_d), band(F.Sb, N, k, n_b, r_nc));
+                                double2 t2 = cmul(band(Hbb, N, k, n_b, r_nc), band(F.Sb, N, k, n_a, n_d));
+                                double2 t12 = cadd(t1, t2);
+                                h1 = cadd(h1, make_double2(t12.x * pi.sgn, t12.y * pi.sgn));
+                            }
+                            re = re + h1.x;
+                            im = im + h1.y;
+                        }
+                        F.Hidx[oH + e] = (int64_t)j + 1;
+                        F.Hdat[oH + e] = make_double2(re, im);
+                    }
+                }
+                oH += tot;
+            }
+            // S runs
+            if (leq || leqx) {
+                int cnt = ss.l1 + ss.l2;
+                int incl = cnt;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(FULL, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                const int excl = incl - cnt;
+                const int tot = __shfl_sync(FULL, incl, 31);
+                for (int e0 = 0; e0 < tot; e0 += 32) {
+                    const int e = e0 + lane;
+                    int pos = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        int cand_pos = pos + step;
+                        int v = __shfl_sync(FULL, excl, cand_pos);
+                        if (v <= e) pos = cand_pos;
+                    }
+                    const int o_ex = __shfl_sync(FULL, excl, pos);
+                    const int r_nc = __shfl_sync(FULL, n_c, pos);
+                    const int r_base = __shfl_sync(FULL, base, pos);
+                    const int r_lo = __shfl_sync(FULL, lo, pos);
+                    const int r_s1 = __shfl_sync(FULL, ss.s1, pos);
+                    const int r_l1 = __shfl_sync(FULL, ss.l1, pos);
+                    const int r_s2 = __shfl_sync(FULL, ss.s2, pos);
+                    if (e < tot) {
+                        const int o = e - o_ex;
+                        const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
+                        const int j = r_base + (n_d - r_lo);
+                        // S_mat_neq (mat_els.f90:664-678)
+                        const int N = A.N;
+                        double2 s1 = make_double2(0.0, 0.0);
+                        if (MIXED && F.ff_one_body) {
+                            FF t{0.f, 0.f};
+                            const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
+                            const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
+                            if (leq && sup) {
+                                float4 a = SA[r_nc - n_a], b = SB[n_d - n_b];
+                                t = ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y));
+                            }
+                            if (leqx && supx) {
+                                float4 a = SA[n_d - n_a], b = SB[r_nc - n_b];
+                                t = ff_add(t, ff_neg_if(ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y)),
+                                                        pi.sgn < 0.0));
+                            }
+                            s1 = make_double2(ff_to_double(t, 0), 0.0);
+                        } else if (F.s_real) {
+                            // real S: the l_eq term lives under sup, l_eq_ex under sup_x
+                            const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
+                            const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
+                            double sr = 0.0;
+                            if (leq && sup) sr = band(F.Sb, N, k, n_a, r_nc).x * band(F.Sb, N, k, n_b, n_d).x;
+                            if (leqx && supx)
+                                sr = fma(pi.sgn * band(F.Sb, N, k, n_a, n_d).x, band(F.Sb, N, k, n_b, r_nc).x, sr);
+                            s1 = make_double2(sr, 0.0);
+                        } else {
+                            if (leq) s1 = cadd(s1, cmul(band(F.Sb, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d)));
+                            if (leqx) {
+                                double2 a = band(F.Sb, N, k, n_a, n_d);
+                                a = make_double2(a.x * pi.sgn, a.y * pi.sgn);
+                                s1 = cadd(s1, cmul(a, band(F.Sb, N, k, n_b, r_nc)));
+                            }
+                        }
+                        F.Sidx[oS + e] = (int64_t)j + 1;
+                        F.Sdat[oS + e] = s1;
+                    }
+                }
+                oS += tot;
+            }
+        }
+    }
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
@@ -507,277 +872,34 @@ __global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs
         for (int i = threadIdx.x; i < A.K1; i += blockDim.x) sexp[i] = F.Rexp[tix * A.K1 + i];
     }
     if (!stage_tile(src, sR, (uint32_t)(F.tile * sizeof(double)), &bar, F.err)) return;
-    const float2 *sR2 = (const float2 *)sR;
+    const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int rr = warp; rr < nrow; rr += nwarp)
+        fill_row<MIXED>(F, srow[rr], sch[rr], n_a, n_b, sR, sexp, sA[warp], sKo[warp]);
+}
 
-    const int k = A.k, W = 2 * k - 1, W2 = W * W, K1 = A.K1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const unsigned FULL = 0xffffffffu;
-    for (int rr = warp; rr < nrow; rr += nwarp) {
-        const int row = srow[rr];
-        const int c_r = sch[rr];
-        const int l_a = A.chl[c_r] >> 8, l_b = A.chl[c_r] & 255;  // row channel (l1, l2)
-        // FP32-pair band rows of this row: X_row[d] = X[n][n+d], |d| < k
-        const size_t ra = (size_t)(n_a - 1) * W + (k - 1), rb = (size_t)(n_b - 1) * W + (k - 1);
-        const float4 *HaA = F.Hbf ? F.Hbf + (size_t)l_a * A.N * W + ra : nullptr;  // H_la[n_a][.]
-        const float4 *HbB = F.Hbf ? F.Hbf + (size_t)l_b * A.N * W + rb : nullptr;  // H_lb[n_b][.]
-        const float4 *SA = F.Sbf ? F.Sbf + ra : nullptr;                           // S[n_a][.]
-        const float4 *SB = F.Sbf ? F.Sbf + rb : nullptr;                           // S[n_b][.]
-        int64_t oH = F.Hptr[row - F.ptr_row0] - 1 - F.Hbase;
-        int64_t oS = F.Sptr[row - F.ptr_row0] - 1 - F.Sbase;
-        for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
-            const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
-            const int flags = pi.flags;
-            const bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
-            const bool Aok = dir_ok || leq || leqx, Bok = ex_ok || leq || leqx;
-            if (!Aok && !Bok) continue;
-            const int nlo = (!A.full && c_c == c_r) ? n_a : 1;
-            const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, Aok, Bok, nlo);
-            const int ncand = cand.l1 + cand.l2;
-            const size_t pbase = ((size_t)c_r * A.n_ch + c_c) * 2 * K1;
-            const int8_t *kd = A.pair_k + pbase;
-            const int8_t *kx = kd + K1;
-            const double *ad = A.pair_a + pbase;
-            const double *ax = ad + K1;
-            int Ed = 0, Ex = 0;
-            if (MIXED) {
-                // scaled multipole weights of this channel pair for this tile
-                int ed = -100000, ex = -100000;
-                if (lane < pi.nd) ed = sexp[kd[lane]];
-                if (lane < pi.nx) ex = sexp[kx[lane]];
-                Ed = ed;
-                Ex = ex;
-                for (int o = 16; o > 0; o >>= 1) {
-                    Ed = max(Ed, __shfl_xor_sync(FULL, Ed, o));
-                    Ex = max(Ex, __shfl_xor_sync(FULL, Ex, o));
-                }
-                if (lane < pi.nd) {
-                    const float *af = A.pair_af + (pbase + lane) * 2;
-                    float sc = pow2f(ed - Ed);
-                    sA[warp][0][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
-                    sKo[warp][0][lane] = kd[lane] * W2;
-                }
-                if (lane < pi.nx) {
-                    const float *af = A.pair_af + (pbase + K1 + lane) * 2;
-                    float sc = pow2f(ex - Ex);
-                    sA[warp][1][lane] = make_float2(__fmul_rn(af[0], sc), __fmul_rn(af[1], sc));
-                    sKo[warp][1][lane] = kx[lane] * W2;
-                }
-                __syncwarp();
-            }
-            for (int g0 = 0; g0 < ncand; g0 += 32) {
-                const int ci = g0 + lane;
-                Iv2 hs{0, 0, 0, 0}, ss{0, 0, 0, 0};
-                int base = 0, lo = 0, n_c = 0;
-                if (ci < ncand) {
-                    n_c = iv2_at(cand, ci);
-                    col_sets(A, c_r, c_c, n_a, n_b, n_c, flags, hs, ss, base, lo);
-                }
-                // H runs
-                {
-                    int cnt = hs.l1 + hs.l2;
-                    int incl = cnt;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        int y = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= o) incl += y;
-                    }
-                    const int excl = incl - cnt;
-                    const int tot = __shfl_sync(FULL, incl, 31);
-                    for (int e0 = 0; e0 < tot; e0 += 32) {
-                        const int e = e0 + lane;
-                        int pos = 0;
-#pragma unroll
-                        for (int step = 16; step > 0; step >>= 1) {
-                            int cand_pos = pos + step;
-                            int v = __shfl_sync(FULL, excl, cand_pos);
-                            if (v <= e) pos = cand_pos;
-                        }
-                        const int o_ex = __shfl_sync(FULL, excl, pos);
-                        const int r_nc = __shfl_sync(FULL, n_c, pos);
-                        const int r_base = __shfl_sync(FULL, base, pos);
-                        const int r_lo = __shfl_sync(FULL, lo, pos);
-                        const int r_s1 = __shfl_sync(FULL, hs.s1, pos);
-                        const int r_l1 = __shfl_sync(FULL, hs.l1, pos);
-                        const int r_s2 = __shfl_sync(FULL, hs.s2, pos);
-                        if (e < tot) {
-                            const int o = e - o_ex;
-                            const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
-                            const int j = r_base + (n_d - r_lo);
-                            const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
-                            const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
-                            double re = 0.0, im = 0.0;
-                            const bool r12 = (sup && dir_ok) || (supx && ex_ok);
-                            const bool one = (sup && leq) || (supx && leqx);
-                            if (MIXED && F.ff_one_body) {
-                                // everything in FP32-pair arithmetic, one rounding to double
-                                FF v{0.f, 0.f};
-                                int Ev = 0;
-                                bool has = false;
-                                if (r12) {
-                                    const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
-                                    const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
-                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
-                                    if (sup)
-                                        for (int u = 0; u < pi.nd; ++u)
-                                            ff_madd(fd, sA[warp][0][u], sR2[sKo[warp][0][u] + od]);
-                                    if (supx)
-                                        for (int u = 0; u < pi.nx; ++u)
-                                            ff_madd(fx, sA[warp][1][u], sR2[sKo[warp][1][u] + ox]);
-                                    v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
-                                    has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
-                                }
-                                FF hi_im{0.f, 0.f};
-                                if (one) {
-                                    // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
-                                    // term is non-zero only under sup, the l_eq_ex term only
-                                    // under sup_x, so both lookups stay inside the band
-                                    FF hr{0.f, 0.f};
-                                    if (leq && sup) {
-                                        const int dc = r_nc - n_a, dd = n_d - n_b;
-                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
-                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
-                                        hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
-                                                    ff_mul(make_float2(h2.x, h2.y), s2r));
-                                        hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
-                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
-                                    }
-                                    if (leqx && supx) {
-                                        const int dc = n_d - n_a, dd = r_nc - n_b;
-                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
-                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
-                                        bool ng = pi.sgn < 0.0;
-                                        FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
-                                                       ff_mul(make_float2(h2.x, h2.y), s2r));
-                                        FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
-                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
-                                        hr = ff_add(hr, ff_neg_if(xr, ng));
-                                        hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
-                                    }
-                                    v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
-                                    has = true;
-                                }
-                                re = has ? ff_to_double(v, Ev - kRkBias) : 0.0;
-                                im = one ? ff_to_double(hi_im, 0) : 0.0;
-                            } else if (r12) {
-                                const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
-                                const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
-                                if (MIXED) {
-                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
-                                    if (sup)
-                                        for (int u = 0; u < pi.nd; ++u)
-                                            ff_madd(fd, sA[warp][0][u], sR2[sKo[warp][0][u] + od]);
-                                    if (supx)
-                                        for (int u = 0; u < pi.nx; ++u)
-                                            ff_madd(fx, sA[warp][1][u], sR2[sKo[warp][1][u] + ox]);
-                                    int Ev;
-                                    FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
-                                    re = ff_to_double(v, Ev - kRkBias);
-                                } else {
-                                    double res = 0.0;
-                                    if (sup) {
-                                        const double *Rt = sR + od;
-                                        double r = 0.0;
-                                        for (int u = 0; u < pi.nd; ++u) r = fma(Rt[kd[u] * W2], ad[u], r);
-                                        res = res + r;
-                                    }
-                                    if (supx) {
-                                        const double *Rt = sR + ox;
-                                        double r = 0.0;
-                                        for (int u = 0; u < pi.nx; ++u) r = fma(Rt[kx[u] * W2], ax[u], r);
-                                        res = res + r;
-                                    }
-                                    re = res;
-                                }
-                            }
-                            if (one && !(MIXED && F.ff_one_body)) {
-                                // H_1p_neq (mat_els.f90:697-715)
-                                const int N = A.N;
-                                const double2 *Ha = F.Hb + (size_t)l_a * N * W;
-                                const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
-                                double2 h1 = make_double2(0.0, 0.0);
-                                if (leq) {
-                                    double2 t1 = cmul(band(Ha, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d));
-                                    double2 t2 = cmul(band(Hbb, N, k, n_b, n_d), band(F.Sb, N, k, n_a, r_nc));
-                                    h1 = cadd(cadd(h1, t1), t2);
-                                }
-                                if (leqx) {
-                                    double2 t1 = cmul(band(Ha, N, k, n_a, n_d), band(F.Sb, N, k, n_b, r_nc));
-                                    double2 t2 = cmul(band(Hbb, N, k, n_b, r_nc), band(F.Sb, N, k, n_a, n_d));
-                                    double2 t12 = cadd(t1, t2);
-                                    h1 = cadd(h1, make_double2(t12.x * pi.sgn, t12.y * pi.sgn));
-                                }
-                                re = re + h1.x;
-                                im = im + h1.y;
-                            }
-                            F.Hidx[oH + e] = (int64_t)j + 1;
-                            F.Hdat[oH + e] = make_double2(re, im);
-                        }
-                    }
-                    oH += tot;
-                }
-                // S runs
-                if (leq || leqx) {
-                    int cnt = ss.l1 + ss.l2;
-                    int incl = cnt;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        int y = __shfl_up_sync(FULL, incl, o);
-                        if (lane >= o) incl += y;
-                    }
-                    const int excl = incl - cnt;
-                    const int tot = __shfl_sync(FULL, incl, 31);
-                    for (int e0 = 0; e0 < tot; e0 += 32) {
-                        const int e = e0 + lane;
-                        int pos = 0;
-#pragma unroll
-                        for (int step = 16; step > 0; step >>= 1) {
-                            int cand_pos = pos + step;
-                            int v = __shfl_sync(FULL, excl, cand_pos);
-                            if (v <= e) pos = cand_pos;
-                        }
-                        const int o_ex = __shfl_sync(FULL, excl, pos);
-                        const int r_nc = __shfl_sync(FULL, n_c, pos);
-                        const int r_base = __shfl_sync(FULL, base, pos);
-                        const int r_lo = __shfl_sync(FULL, lo, pos);
-                        const int r_s1 = __shfl_sync(FULL, ss.s1, pos);
-                        const int r_l1 = __shfl_sync(FULL, ss.l1, pos);
-                        const int r_s2 = __shfl_sync(FULL, ss.s2, pos);
-                        if (e < tot) {
-                            const int o = e - o_ex;
-                            const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
-                            const int j = r_base + (n_d - r_lo);
-                            // S_mat_neq (mat_els.f90:664-678)
-                            const int N = A.N;
-                            double2 s1 = make_double2(0.0, 0.0);
-                            if (MIXED && F.ff_one_body) {
-                                FF t{0.f, 0.f};
-                                const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
-                                const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
-                                if (leq && sup) {
-                                    float4 a = SA[r_nc - n_a], b = SB[n_d - n_b];
-                                    t = ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y));
-                                }
-                                if (leqx && supx) {
-                                    float4 a = SA[n_d - n_a], b = SB[r_nc - n_b];
-                                    t = ff_add(t, ff_neg_if(ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y)),
-                                                            pi.sgn < 0.0));
-                                }
-                                s1 = make_double2(ff_to_double(t, 0), 0.0);
-                            } else {
-                                if (leq) s1 = cadd(s1, cmul(band(F.Sb, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d)));
-                                if (leqx) {
-                                    double2 a = band(F.Sb, N, k, n_a, n_d);
-                                    a = make_double2(a.x * pi.sgn, a.y * pi.sgn);
-                                    s1 = cadd(s1, cmul(a, band(F.Sb, N, k, n_b, r_nc)));
-                                }
-                            }
-                            F.Sidx[oS + e] = (int64_t)j + 1;
-                            F.Sdat[oS + e] = s1;
-                        }
-                    }
-                    oS += tot;
-                }
-            }
-        }
+// Row mode, for row ranges inside one or two channels, where a tile holds a
+// single row of the range: a warp per row, and the row's R^k tile read through
+// L1/L2 instead of staged (a staged tile would serve one warp and cap the SM
+// at a few CTAs).
+template <bool MIXED>
+__global__ void __launch_bounds__(128, 6) k_csr_fill_rows(FillArgs F) {
+    __shared__ int sexpw[4][kMaxK1];
+    __shared__ float2 sA[4][2][kMaxK1];
+    __shared__ int sKo[4][2][kMaxK1];
+    const BlockArgs &A = F.B;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row = F.row0 + (int64_t)blockIdx.x * 4 + warp;
+    if (row >= F.row1) return;  // whole warp
+    const bs2e_config cf = A.cfg[row];
+    const int n_a = (int)cf.n1, n_b = (int)cf.n2;
+    const int c_r = A.lmap[cf.l1 * kMaxL + cf.l2];
+    const size_t tix = (size_t)(n_a - 1) * A.N + (n_b - 1);
+    const double *R = MIXED ? (const double *)(F.Rf + tix * F.tile) : F.R + tix * F.tile;
+    if (MIXED) {
+        for (int i = lane; i < A.K1; i += 32) sexpw[warp][i] = F.Rexp[tix * A.K1 + i];
+        __syncwarp();
     }
+    fill_row<MIXED>(F, (int)row, c_r, n_a, n_b, R, sexpw[warp], sA[warp], sKo[warp]);
 }
 
 }  // namespace
@@ -907,6 +1029,15 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     F.Sbase = r.Sbase;
     F.a0 = r.a0;
     size_t smem = fill_smem(h->g);
+    if (h->plan.n_config > 0 && r.row1 > r.row0 && r.rows_mode) {
+        const unsigned grid = (unsigned)((r.row1 - r.row0 + 3) / 4);
+        if (h->precision == BS2E_PREC_MIXED)
+            k_csr_fill_rows<true><<<grid, 128, 0, h->stream>>>(F);
+        else
+            k_csr_fill_rows<false><<<grid, 128, 0, h->stream>>>(F);
+        h->launches++;
+        return;
+    }
     if (h->plan.n_config > 0 && r.row1 > r.row0 && r.a1 >= r.a0) {
         const unsigned tiles = (unsigned)((int64_t)(r.a1 - r.a0 + 1) * h->g.N);
         if (h->precision == BS2E_PREC_MIXED) {

@@ -29,7 +29,10 @@ namespace bs2e {
 constexpr int kMaxOrder = 16;  // B-spline order limit (the reference allows 20 in BVALUE_D)
 constexpr int kMaxGL = 32;     // Gauss-Legendre points per interval
 constexpr int kMaxK1 = 32;     // multipoles 0..31
-constexpr int kRkBias = 96;    // mixed R^k store: a slice maximum is scaled to [2^96, 2^97)
+// mixed R^k store: a slice maximum is scaled to [2^112, 2^113).  Weighted sums
+// in the fill (angular weights below 2^3, at most 32 terms) stay below 2^120;
+// values 2^214 below the maximum keep both FP32 words normal.
+constexpr int kRkBias = 112;
 
 // Per (row channel, column channel) coupling of one symmetry block.
 struct PairInfo {
@@ -135,7 +138,7 @@ struct bs2e_handle {
     // one-body, banded complex: Hb[l][x][W], Sb[x][W]
     double2 *d_Hb = nullptr, *d_Sb = nullptr;
     float4 *d_Hbf = nullptr, *d_Sbf = nullptr;  // same bands as FP32 pairs (mixed path)
-    int *d_flag = nullptr;                      // band values outside the FP32-pair range
+    unsigned long long *d_range = nullptr;      // min / max magnitude of the H and S bands
     int64_t n_l = 0;
     bool have_one_body = false;
     bool s_real = true;
@@ -164,7 +167,7 @@ struct bs2e_handle {
     int64_t rptr_cap = 0;
     unsigned char *d_stage[2] = {nullptr, nullptr};
     int64_t stage_cap = 0;
-    int64_t stage_limit = (int64_t)2 << 30;
+    int64_t stage_limit = (int64_t)8 << 30;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_filled[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     // mat-vec staging for host operands, and its bad-input flag word
@@ -251,9 +254,13 @@ void launch_plan_seg_on(bs2e_handle *h, const bs2e_config *cfg, int64_t n, const
 void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64_t *ptr);
 // Rows [row0, row1) of the counted block; their tiles have n_a in [a0, a1].
 // Row r's entries start at output position ptr[r - ptr_row0] - 1 - base.
+// rows_mode: a warp per row with the R^k tile read through L1/L2 (ranges
+// inside one or two channels, where each tile holds a single row of the
+// range) instead of a CTA per staged tile.
 struct FillRange {
     int64_t row0 = 0, row1 = 0, ptr_row0 = 0, Hbase = 0, Sbase = 0;
     int a0 = 1, a1 = 0;
+    bool rows_mode = false;
 };
 // 1-based CSR pointers of rows [row0, row0 + n) (n + 1 entries, starting at 1)
 void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr, int64_t row0,

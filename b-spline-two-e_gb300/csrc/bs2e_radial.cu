@@ -231,8 +231,9 @@ __global__ void k_totals(RadialDev P) {
 //
 // MIXED stores each (tile, k) slice as FP32 pairs (hi, lo) of R 2^(kRkBias-e)
 // with e = ilogb(max of the slice), and e in Rexp[tile][k]: hi + lo carries
-// ~48 bits, and a slice may span up to ~2^180 before its smallest values lose
-// precision (2^108 at the N=200, k=0..10 grid).
+// ~48 bits, and a slice may span up to ~2^214 before its smallest values lose
+// precision (2^108 at the N=200, k=0..10 grid; about 2^200 at k=20 on the
+// N=800, r_max=800 grid).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double rk_element(const double *__restrict__ mom,
                                             const double *__restrict__ dint,
@@ -596,20 +597,34 @@ __global__ void k_one_body(const double *__restrict__ knots, const double *__res
 }
 
 // Splits the complex FP64 bands into FP32 pairs (re hi, re lo, im hi, im lo)
-// for the mixed assembly; flags any non-zero magnitude outside [2^-100, 2^100]
-// so the host can keep FP64 one-body products instead.
+// for the mixed assembly, and reduces the smallest and largest non-zero
+// magnitude of the real and imaginary parts into range[0..1] (bit patterns of
+// positive doubles order like integers); the host enables the FP32-pair
+// products only if every product of two band values, and its TwoProd error
+// terms, stays normal FP32.
 __global__ void k_band_split(const double2 *__restrict__ src, int64_t n, float4 *__restrict__ dst,
-                             int *__restrict__ flag) {
+                             unsigned long long *__restrict__ range) {
+    unsigned long long mn = 0x7ff0000000000000ull, mx = 0ull;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
          e += (int64_t)gridDim.x * blockDim.x) {
         double2 v = src[e];
         float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
         float rl = __double2float_rn(v.x - (double)rh), il = __double2float_rn(v.y - (double)ih);
         dst[e] = make_float4(rh, rl, ih, il);
-        double ar = fabs(v.x), ai = fabs(v.y);
-        const double lo = 7.888609052210118e-31, hi = 1.2676506002282294e+30;  // 2^-100, 2^100
-        if ((ar != 0.0 && (ar < lo || ar > hi)) || (ai != 0.0 && (ai < lo || ai > hi)))
-            atomicOr(flag, 1);
+        const unsigned long long br = (unsigned long long)__double_as_longlong(fabs(v.x));
+        const unsigned long long bi = (unsigned long long)__double_as_longlong(fabs(v.y));
+        if (br) {
+            mn = min(mn, br);
+            mx = max(mx, br);
+        }
+        if (bi) {
+            mn = min(mn, bi);
+            mx = max(mx, bi);
+        }
+    }
+    if (mx) {
+        atomicMin(&range[0], mn);
+        atomicMax(&range[1], mx);
     }
 }
 
@@ -753,9 +768,11 @@ void launch_rk_slice(bs2e_handle *h, int kk, double *d_out) {
 void launch_band_split(bs2e_handle *h) {
     const Radial &g = h->g;
     int64_t nh = h->n_l * g.N * g.W, ns = (int64_t)g.N * g.W;
-    cudaMemsetAsync(h->d_flag, 0, sizeof(int), h->stream);
-    k_band_split<<<grid_for(nh, 256), 256, 0, h->stream>>>(h->d_Hb, nh, h->d_Hbf, h->d_flag);
-    k_band_split<<<grid_for(ns, 256), 256, 0, h->stream>>>(h->d_Sb, ns, h->d_Sbf, h->d_flag);
+    const unsigned long long init[4] = {0x7ff0000000000000ull, 0ull, 0x7ff0000000000000ull, 0ull};
+    cudaMemcpyAsync(h->d_range, init, sizeof(init), cudaMemcpyHostToDevice, h->stream);
+    k_band_split<<<grid_for(nh, 256), 256, 0, h->stream>>>(h->d_Hb, nh, h->d_Hbf, h->d_range);
+    k_band_split<<<grid_for(ns, 256), 256, 0, h->stream>>>(h->d_Sb, ns, h->d_Sbf, h->d_range + 2);
+    cudaStreamSynchronize(h->stream);  // init lives on this stack frame
     h->launches += 2;
 }
 

@@ -22,12 +22,18 @@ namespace {
 
 // acc += a x in complex FP64.  The imaginary part of most entries is zero
 // (the two-electron and overlap terms are real; only the CAP one-body term is
-// complex), so its two FMAs run only where it is not: the FP64 pipe, not
-// HBM, bounds this kernel otherwise.
+// complex), and the FP64 pipe, not HBM, bounds this kernel: a warp whose
+// entries are all real (tested on the bit pattern, an integer op, and voted
+// across the warp so that no predicated FMAs are issued) runs two FMAs per
+// entry instead of four.
 __device__ __forceinline__ void cmac(double &re, double &im, double2 a, double2 x) {
     re = fma(a.x, x.x, re);
     im = fma(a.x, x.y, im);
-    if (a.y != 0.0) {
+    const bool cplx = (__double_as_longlong(a.y) << 1) != 0;  // +-0 count as real
+    if (__any_sync(__activemask(), cplx)) {
+        // a compiler barrier keeps this a branch: predicated FMAs would still
+        // occupy the FP64 pipe
+        asm volatile("" ::: "memory");
         re = fma(-a.y, x.y, re);
         im = fma(a.y, x.x, im);
     }

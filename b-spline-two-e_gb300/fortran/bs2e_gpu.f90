@@ -18,7 +18,7 @@ module bs2e_gpu
 
     type, bind(C) :: bs2e_opts_c
         integer(c_int64_t) :: precision, device
-        integer(c_int64_t) :: stage_bytes    ! HBM staging per area for host-array fills (0 = 2 GiB)
+        integer(c_int64_t) :: stage_bytes    ! HBM staging per area for host-array fills (0 = 8 GiB)
         integer(c_int64_t) :: reserved(5)
     end type bs2e_opts_c
 

@@ -65,7 +65,7 @@ typedef struct {
     int64_t precision; /* BS2E_PREC_FP64 (default) or BS2E_PREC_MIXED */
     int64_t device;    /* CUDA device ordinal (default 0) */
     int64_t stage_bytes; /* size of each of the two HBM staging areas of fills
-                            into host arrays (0 = 2 GiB) */
+                            into host arrays (0 = 8 GiB) */
     int64_t reserved[5];
 } bs2e_opts;
 
@@ -270,7 +270,7 @@ BS2E_API bs2e_status bs2e_write_block(const char *path, int64_t n_rows_b, int64_
  * 1-based column indices, exactly the rows row_first.. of bs2e_block_fill_ex.
  * With host outputs (out_on_device = 0), here and in bs2e_block_fill[_ex],
  * the rows are assembled in chunks through two staging areas of at most
- * 2 GiB each in HBM, the device-to-host copy of one chunk overlapping the
+ * 8 GiB each in HBM, the device-to-host copy of one chunk overlapping the
  * assembly of the next.  No counterpart in the reference (its blocks are
  * built whole, hamiltonian.f90:106-283). */
 BS2E_API bs2e_status bs2e_block_count_rows(bs2e_handle *h, const bs2e_config *configs,

@@ -18,6 +18,14 @@ CASES = {
                    spins=(0, 1), Z=2),
     "cut": dict(k=5, n_b=24, r_max=20.0, q=7, max_k=3, lmax=3, max_L=2, z_pol=False,
                 spins=(0,), Z=2, max_n_b=15, n_all_l=12, l2_max=1),
+    # radii to 1e5 a.u.: R^k slice maxima far below 2^-12, where the mixed
+    # path joins the one-body and two-electron parts in FP64
+    "wide": dict(k=6, n_b=28, r_max=1.0e5, q=8, max_k=6, lmax=2, max_L=1, z_pol=True,
+                 spins=(0, 1), Z=2),
+    # order 9 with k=0..14: 35 KB R^k tiles, where ranges inside one channel
+    # run the fill a warp per row
+    "bigtile": dict(k=9, n_b=24, r_max=30.0, q=9, max_k=14, lmax=2, max_L=1, z_pol=True,
+                    spins=(0,), Z=2),
 }
 
 

@@ -172,7 +172,7 @@ def test_gpu_hydrogenic_known_answer(bs2e, oracle):
 MIXED_RTOL = 1e-11
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2"])
+@pytest.mark.parametrize("case", ["cfg1", "small2", "wide"])
 def test_mixed_rk_store_matches_oracle(bs2e, oracle, case):
     c = CASES[case]
     R = oracle_reference(case)["R"]
@@ -188,7 +188,7 @@ def test_mixed_rk_store_matches_oracle(bs2e, oracle, case):
     np.testing.assert_allclose(got, oracle.rk_lookup(R, k, keys), rtol=1e-13, atol=0)
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "cut"])
+@pytest.mark.parametrize("case", ["cfg1", "small2", "cut", "wide"])
 def test_mixed_blocks_match_oracle(bs2e, oracle, case):
     c = CASES[case]
     ref = oracle_reference(case)

@@ -102,3 +102,71 @@ def test_precision_report(bs2e, oracle):
     s = rep["summary"]
     assert s["rk_fp64_max"] <= 1e-12 and s["H_fp64_max"] <= 1e-12
     assert s["rk_mixed_max"] <= 1e-9 and s["H_mixed_max"] <= 1e-9
+
+
+WL5 = dict(k=9, n_b=800, r_max=800.0, q=12, max_k=20, lmax=10, max_L=5, Z=2)
+
+
+@pytest.mark.skipif(not RUN, reason="set BS2E_PRECISION_REPORT=1 (runs for minutes)")
+def test_precision_report_large(bs2e, oracle):
+    """The large configuration (order 9, N=800, r_max=800, q=12, k=0..20,
+    l_max=10, singlet L=0..5).  The oracle's primitives would take hours at
+    this size, so the oracle assembles the sampled rows (construct_block, with
+    its term-magnitude scale) from the GPU's FP64 R^k store, exported to the
+    host, and the oracle's one-body matrices, which both GPU handles also
+    use: this checks the FP64 and the mixed assembly, and the mixed store,
+    on the blocks of the large configuration."""
+    w = WL5
+    k, N, q, K1 = w["k"], w["n_b"], w["q"], w["max_k"] + 1
+    t = bs2e.grids.explin_knots(k, N, w["r_max"])
+    H1p = oracle.setup_H1p(t, k, q, w["Z"], w["lmax"] + 1, cap_order=2, cap_r0=10.0,
+                           cap_eta=1e-3)
+    S = oracle.setup_S(t, k, q)
+    hd = bs2e.Bs2e(t, k, q, w["max_k"], precision=bs2e.PREC_FP64)
+    hm = bs2e.Bs2e(t, k, q, w["max_k"], precision=bs2e.PREC_MIXED)
+    for h in (hd, hm):
+        h.slater()
+        h.rk()
+        h.set_one_body(H1p, S)
+    W = 2 * k - 1
+    R = np.zeros((N, N, W, W, K1))
+    rk_mixed = []
+    for kk in range(K1):
+        R[..., kk] = hd.rk_export(kk)
+        m = hm.rk_export(kk)
+        ref = R[..., kk]
+        mask = ref != 0.0
+        rk_mixed.append(float((np.abs(m[mask] - ref[mask]) / ref[mask]).max()))
+        del m
+    rep = {"workload": "order 9, N=800, r_max=800, q=12, k=0..20, l_max=10, singlet L=0..5",
+           "rk_mixed_vs_fp64_max_per_k": rk_mixed}
+    rows_rep = []
+    for L in range(w["max_L"] + 1):
+        cf = bs2e.configs(L, L % 2, w["lmax"], N, k)
+        n = cf.size
+        for frac in (0.1, 0.55, 0.93):
+            r0 = int(frac * n)
+            r1 = r0 + 6
+            Hr, Sr = oracle.construct_block(cf, L, k, N, w["max_k"], R, H1p, S, True, 0,
+                                            rows=(r0, r1))
+            ent = {"L": L, "rows": [r0, r1], "nnz_H": int(Hr["nnz"])}
+            for name, h in (("fp64", hd), ("mixed", hm)):
+                H, Sg = h.block_rows(cf, L, r0, r1 - r0, True, 0)
+                np.testing.assert_array_equal(H["indices"], Hr["indices"])
+                np.testing.assert_array_equal(Sg["indices"], Sr["indices"])
+                sc = np.maximum(Hr["scale"], 1e-300)
+                ent["H_" + name + "_max"], ent["H_" + name + "_rms"] = _rel_stats(
+                    H["data"], Hr["data"], sc)
+            rows_rep.append(ent)
+    hd.close()
+    hm.close()
+    rep["H_rows"] = rows_rep
+    rep["summary"] = {"rk_mixed_max": max(rk_mixed),
+                      "H_fp64_max": max(e["H_fp64_max"] for e in rows_rep),
+                      "H_mixed_max": max(e["H_mixed_max"] for e in rows_rep)}
+    out = os.environ.get("BS2E_REPORT_OUT_LARGE")
+    if out:
+        with open(out, "w") as f:
+            json.dump(rep, f, indent=1)
+    s = rep["summary"]
+    assert s["H_fp64_max"] <= 1e-12 and s["H_mixed_max"] <= 1e-9 and s["rk_mixed_max"] <= 1e-9

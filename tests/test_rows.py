@@ -118,3 +118,37 @@ def test_row_range_errors(bs2e):
         # the handle stays usable
         n_h, n_s = h.block_count_rows(cf, L, 0, 3, True, spin)
         assert n_h > 0
+
+
+def test_row_mode_on_large_tiles(bs2e, oracle):
+    """Order 9 with k=0..14 (35 KB R^k tiles): ranges inside one channel run a
+    warp per row with the tile read through L1/L2; ranges across channels and
+    whole blocks keep the staged tiles.  Both must give the oracle's rows."""
+    c = CASES["bigtile"]
+    ref = oracle_reference("bigtile")
+    for prec, tol in ((0, RTOL), (bs2e.PREC_MIXED, 1e-11)):
+        h = bs2e.Bs2e(ref["knots"], c["k"], c["q"], c["max_k"], precision=prec,
+                      stage_bytes=96 << 10)
+        try:
+            h.slater()
+            h.rk()
+            h.set_one_body(ref["H1p"], ref["S"])
+            for (L, M, par, spin, cf) in blocks(bs2e, "bigtile"):
+                n = cf.size
+                ch = cf["l1"] * 100 + cf["l2"]
+                ends = np.flatnonzero(np.diff(ch)) + 1
+                first_end = int(ends[0]) if ends.size else n  # end of the first channel
+                for (r0, r1) in [(3, min(first_end, 60)), (0, n)]:
+                    H, S = h.block_rows(cf, L, r0, r1 - r0, True, spin)
+                    Hr, Sr = oracle.construct_block(cf, L, c["k"], c["n_b"], c["max_k"], ref["R"],
+                                                    ref["H1p"], ref["S"], True, spin,
+                                                    rows=(r0, r1))
+                    assert_csr_close(H, Hr, tol)
+                    assert_csr_close(S, Sr, tol, with_scale=False)
+                # a whole block through 96 KiB staging areas (chunks inside channels)
+                H, S = h.block(cf, L, True, spin)
+                Hr, Sr = oracle.construct_block(cf, L, c["k"], c["n_b"], c["max_k"], ref["R"],
+                                                ref["H1p"], ref["S"], True, spin)
+                assert_csr_close(H, Hr, tol)
+        finally:
+            h.close()
