@@ -2,12 +2,13 @@
 //
 // A ragged batch (each basis with its own order, spline count, knot grid and
 // multipole range) runs bs2e_slater + bs2e_rk of every handle as four
-// persistent kernels (tabulation, moments, pair totals, R^k store), each
-// draining one work queue that spans all problems, so small problems do not
-// leave the GPU idle and there is one launch per stage instead of one per
-// problem and stage.  The first run tunes the R^k stage (threads per CTA,
-// items taken per queue access) by timing each candidate; the four stages are
-// then captured once in a CUDA graph and later runs replay it.  Results are
+// persistent kernels (tabulation, moments, pair totals, R^k store of the
+// FP64 and of the mixed problems), each draining one work queue that spans
+// all problems, so small problems do not leave the GPU idle and there is one
+// launch per stage instead of one per problem and stage.  The first run tunes
+// the R^k stage (threads per CTA, items taken per queue access) by timing
+// each candidate; the stages are then captured once in a CUDA graph and later
+// runs replay it.  Results are
 // bit-identical to the per-handle path: both run the same device functions.
 //
 // Reference: setup_Slater_integrals and compute_R_k_map
@@ -31,12 +32,12 @@ struct bs2e_batch {
     int device = 0;
     cudaStream_t stream = nullptr;
     RadialDev *d_probs = nullptr;
-    int64_t *d_off = nullptr;                // 4 stages x (n + 1)
-    unsigned long long *d_counter = nullptr;  // 4 counters
-    std::vector<int64_t> off[4];
-    size_t smem[4] = {0, 0, 0, 0};
-    int threads[4] = {128, 256, 256, 256};
-    int grid[4] = {1, 1, 1, 1};
+    int64_t *d_off = nullptr;                // kStages x (n + 1)
+    unsigned long long *d_counter = nullptr;  // kStages counters
+    std::vector<int64_t> off[5];
+    size_t smem[5] = {0, 0, 0, 0, 0};
+    int threads[5] = {128, 256, 256, 256, 256};
+    int grid[5] = {1, 1, 1, 1, 1};
     int chunk = 1;
     int persistent = 1;  // R^k stage: queue-draining CTAs (1) or one CTA per chunk (0)
     int sms = 0;
@@ -50,6 +51,7 @@ struct bs2e_batch {
 namespace {
 
 constexpr int kTotThreads = 256;
+constexpr int kStages = 5;  // tabulate, moments, totals, R^k FP64, R^k mixed
 
 // Locks every handle of the batch (in address order, so two batches sharing
 // handles cannot deadlock).
@@ -94,13 +96,14 @@ void enqueue_stage(bs2e_batch *b, int stage, int chunk, int persistent = 1) {
     const int n = (int)b->hs.size();
     launch_radial_batch(b->stream, stage, b->grid[stage], b->threads[stage], b->smem[stage],
                         b->d_probs, b->d_off + (size_t)stage * (n + 1), n, b->d_counter + stage,
-                        stage == 3 ? chunk : 1, stage == 3 ? persistent : 1);
+                        stage >= 3 ? chunk : 1, stage >= 3 ? persistent : 1);
     b->launches++;
 }
 
 void enqueue_all(bs2e_batch *b) {
-    cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(unsigned long long), b->stream);
-    for (int st = 0; st < 4; ++st) enqueue_stage(b, st, b->chunk, b->persistent);
+    cudaMemsetAsync(b->d_counter, 0, kStages * sizeof(unsigned long long), b->stream);
+    for (int st = 0; st < kStages; ++st)
+        if (b->off[st].back() > 0) enqueue_stage(b, st, b->chunk, b->persistent);
 }
 
 // Times the R^k stage for each candidate (threads per CTA x work
@@ -110,7 +113,8 @@ bs2e_status tune(bs2e_batch *b) {
     struct Cand {
         int persistent, chunk;
     };
-    const int cand_threads[3] = {128, 256, 512};
+    const int cand_threads[2] = {128, 256};
+    const int ts = b->off[3].back() > 0 ? 3 : 4;  // the R^k stage that is timed
     const Cand cand[5] = {{1, 1}, {1, 2}, {1, 8}, {0, 1}, {0, 4}};
     cudaEvent_t e0, e1;
     BCU(cudaEventCreate(&e0));
@@ -119,11 +123,11 @@ bs2e_status tune(bs2e_batch *b) {
     int bt = 256, bc = 1, bp = 1;
     for (int t : cand_threads)
         for (const Cand &c : cand) {
-            b->threads[3] = t;
-            set_grid(b, 3, c.chunk, c.persistent);
-            BCU(cudaMemsetAsync(b->d_counter + 3, 0, sizeof(unsigned long long), b->stream));
+            b->threads[ts] = t;
+            set_grid(b, ts, c.chunk, c.persistent);
+            BCU(cudaMemsetAsync(b->d_counter + ts, 0, sizeof(unsigned long long), b->stream));
             BCU(cudaEventRecord(e0, b->stream));
-            enqueue_stage(b, 3, c.chunk, c.persistent);
+            enqueue_stage(b, ts, c.chunk, c.persistent);
             BCU(cudaEventRecord(e1, b->stream));
             BCU(cudaEventSynchronize(e1));
             BCU(cudaGetLastError());
@@ -138,11 +142,18 @@ bs2e_status tune(bs2e_batch *b) {
         }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    b->threads[3] = bt;
+    b->threads[3] = b->threads[4] = bt;
     b->chunk = bc;
     b->persistent = bp;
     set_grid(b, 3, bc, bp);
+    set_grid(b, 4, bc, bp);
     b->tuned = true;
+    // the other R^k stage, if the batch has one, runs once with the choice
+    if (ts == 3 && b->off[4].back() > 0) {
+        BCU(cudaMemsetAsync(b->d_counter + 4, 0, sizeof(unsigned long long), b->stream));
+        enqueue_stage(b, 4, bc, bp);
+        BCU(cudaGetLastError());
+    }
     return BS2E_OK;
 }
 
@@ -190,7 +201,7 @@ BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, b
             b->sms = prop.multiProcessorCount;
             BCU(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
             std::vector<RadialDev> probs;
-            for (int s = 0; s < 4; ++s) b->off[s].assign(1, 0);
+            for (int s = 0; s < kStages; ++s) b->off[s].assign(1, 0);
             for (bs2e_handle *h : b->hs) {
                 BCU(cudaStreamSynchronize(h->stream));
                 const Radial &g = h->g;
@@ -201,24 +212,27 @@ BS2E_API bs2e_status bs2e_batch_create(bs2e_handle *const *handles, int64_t n, b
                 } else if (!h->d_R) {
                     BCU(cudaMalloc(&h->d_R, sizeof(double) * (size_t)g.N * g.N * g.tile));
                 }
-                b->smem[3] = std::max(b->smem[3], rk_store_smem(g, mixed));
+                const int rs = mixed ? 4 : 3;
+                b->smem[rs] = std::max(b->smem[rs], rk_store_smem(g, mixed));
                 b->smem[1] = std::max(b->smem[1], moments_smem(g));
                 probs.push_back(radial_dev(h));
-                const int64_t items[4] = {g.n_iv, (int64_t)g.n_iv * g.K1,
-                                          ((int64_t)2 * g.K1 * g.N * g.W + kTotThreads - 1) / kTotThreads,
-                                          (int64_t)g.N * g.N};
-                for (int s = 0; s < 4; ++s) b->off[s].push_back(b->off[s].back() + items[s]);
+                const int64_t tiles = (int64_t)g.N * g.N;
+                const int64_t items[kStages] = {
+                    g.n_iv, (int64_t)g.n_iv * g.K1,
+                    ((int64_t)2 * g.K1 * g.N * g.W + kTotThreads - 1) / kTotThreads,
+                    mixed ? 0 : tiles, mixed ? tiles : 0};
+                for (int s = 0; s < kStages; ++s) b->off[s].push_back(b->off[s].back() + items[s]);
             }
             b->threads[2] = kTotThreads;
             const size_t nn = b->hs.size();
             BCU(cudaMalloc(&b->d_probs, sizeof(RadialDev) * nn));
-            BCU(cudaMalloc(&b->d_off, sizeof(int64_t) * 4 * (nn + 1)));
-            BCU(cudaMalloc(&b->d_counter, 4 * sizeof(unsigned long long)));
+            BCU(cudaMalloc(&b->d_off, sizeof(int64_t) * kStages * (nn + 1)));
+            BCU(cudaMalloc(&b->d_counter, kStages * sizeof(unsigned long long)));
             BCU(cudaMemcpy(b->d_probs, probs.data(), sizeof(RadialDev) * nn, cudaMemcpyHostToDevice));
-            for (int s = 0; s < 4; ++s)
+            for (int s = 0; s < kStages; ++s)
                 BCU(cudaMemcpy(b->d_off + (size_t)s * (nn + 1), b->off[s].data(),
                                sizeof(int64_t) * (nn + 1), cudaMemcpyHostToDevice));
-            for (int s = 0; s < 4; ++s) set_grid(b, s);
+            for (int s = 0; s < kStages; ++s) set_grid(b, s);
             BCU(cudaGetLastError());
             return BS2E_OK;
         };
@@ -238,9 +252,9 @@ BS2E_API bs2e_status bs2e_batch_run(bs2e_batch *b) {
     cudaSetDevice(b->device);
     for (bs2e_handle *h : b->hs) BCU(cudaStreamSynchronize(h->stream));
     if (!b->tuned) {
-        // first run: stages 0-2 eagerly, then every candidate of stage 3
-        // (each a complete R^k pass), then the graph of all four stages
-        BCU(cudaMemsetAsync(b->d_counter, 0, 4 * sizeof(unsigned long long), b->stream));
+        // first run: stages 0-2 eagerly, then every candidate of an R^k stage
+        // (each a complete pass), the other R^k stage once, then the graph
+        BCU(cudaMemsetAsync(b->d_counter, 0, kStages * sizeof(unsigned long long), b->stream));
         for (int s = 0; s < 3; ++s) enqueue_stage(b, s, 1);
         BCU(cudaGetLastError());
         bs2e_status st = tune(b);
@@ -257,7 +271,7 @@ BS2E_API bs2e_status bs2e_batch_run(bs2e_batch *b) {
         return BS2E_OK;
     }
     BCU(cudaGraphLaunch(b->exec, b->stream));
-    b->launches += 4;
+    for (int st = 0; st < kStages; ++st) b->launches += b->off[st].back() > 0 ? 1 : 0;
     BCU(cudaStreamSynchronize(b->stream));
     BCU(cudaGetLastError());
     mark_done(b);

@@ -423,8 +423,11 @@ __global__ void k_rk_store_mixed(RadialDev P, int k_first, int k_count) {
 // Batched radial stage: one persistent kernel per stage runs that stage of
 // every problem of a batch.  Items [off[p], off[p+1]) belong to problem p
 // (0: intervals, 1: (interval, multipole), 2: chunks of blockDim totals,
-// 3: R^k tiles); a CTA takes `chunk` consecutive items per atomicAdd on the
-// stage's counter until the queue is empty.  No CTA waits on another.
+// 3: R^k tiles of the FP64 problems, 4: R^k tiles of the mixed ones); a CTA
+// takes `chunk` consecutive items per atomicAdd on the stage's counter until
+// the queue is empty.  No CTA waits on another.  The R^k stages are separate
+// kernels per store type and capped at 64 registers (256 threads, 4 CTAs per
+// SM), the occupancy of the single-problem k_rk_store.
 // ---------------------------------------------------------------------------
 struct BatchStage {
     const RadialDev *probs;
@@ -447,7 +450,7 @@ __device__ __forceinline__ int find_problem(const int64_t *off, int n, int64_t i
 }
 
 template <int STAGE>
-__global__ void k_radial_batch(BatchStage B) {
+__device__ __forceinline__ void batch_body(const BatchStage &B) {
     extern __shared__ double sm[];
     __shared__ int sexp[kMaxK1];
     __shared__ unsigned long long s_it;
@@ -475,16 +478,26 @@ __global__ void k_radial_batch(BatchStage B) {
             } else if (STAGE == 2) {
                 const int64_t e = li * blockDim.x + threadIdx.x;
                 if (e < totals_count(P)) totals_elem(P, e);
+            } else if (STAGE == 3) {
+                rk_tile_fp64(P, li, 0, P.K1, sm);
+                __syncthreads();
             } else {
-                if (P.mixed)
-                    rk_tile_mixed(P, li, 0, P.K1, sm, sexp,
-                                  sm + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
-                else
-                    rk_tile_fp64(P, li, 0, P.K1, sm);
+                rk_tile_mixed(P, li, 0, P.K1, sm, sexp,
+                              sm + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
                 __syncthreads();
             }
         }
     }
+}
+
+template <int STAGE>
+__global__ void k_radial_batch(BatchStage B) {
+    batch_body<STAGE>(B);
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(256, 4) k_radial_batch_rk(BatchStage B) {
+    batch_body<STAGE>(B);
 }
 
 __global__ void k_rk_gather(const double *__restrict__ R, const float2 *__restrict__ Rf,
@@ -716,7 +729,8 @@ static const void *batch_kernel(int stage) {
         case 0: return (const void *)k_radial_batch<0>;
         case 1: return (const void *)k_radial_batch<1>;
         case 2: return (const void *)k_radial_batch<2>;
-        default: return (const void *)k_radial_batch<3>;
+        case 3: return (const void *)k_radial_batch_rk<3>;
+        default: return (const void *)k_radial_batch_rk<4>;
     }
 }
 
@@ -744,7 +758,8 @@ void launch_radial_batch(cudaStream_t s, int stage, int grid, int threads, size_
         case 0: k_radial_batch<0><<<grid, threads, smem, s>>>(B); break;
         case 1: k_radial_batch<1><<<grid, threads, smem, s>>>(B); break;
         case 2: k_radial_batch<2><<<grid, threads, smem, s>>>(B); break;
-        default: k_radial_batch<3><<<grid, threads, smem, s>>>(B); break;
+        case 3: k_radial_batch_rk<3><<<grid, threads, smem, s>>>(B); break;
+        default: k_radial_batch_rk<4><<<grid, threads, smem, s>>>(B); break;
     }
 }
 

@@ -58,27 +58,48 @@ __global__ void __launch_bounds__(256) k_csr_mv(int64_t n_rows, int64_t n_cols, 
     }
     double re = 0.0, im = 0.0;
     const double2 xr = (OP != 0) ? x[row] : make_double2(0.0, 0.0);
-    for (int64_t j = j0 + lane; j < j1; j += 32) {
-        const int64_t c = idx[j] - 1;
-        const double2 a = A[j];
+    // one entry of the row: c = idx - 1, a = A
+    auto entry = [&](int64_t cc, double2 a) {
+        const int64_t c = cc - 1;
         if (c < 0 || c >= n_cols) {
             atomicOr(bad, 2);
-            continue;
+            return;
         }
         if (OP == 1) {
             double tr = 0.0, ti = 0.0;
             cmac(tr, ti, a, xr);
             atomicAdd(&y[c].x, tr);
             atomicAdd(&y[c].y, ti);
-            continue;
+            return;
         }
-        if (OP == 2 && c < row) continue;
+        if (OP == 2 && c < row) return;
         cmac(re, im, a, x[c]);
         if (OP == 2 && c > row) {
             double tr = 0.0, ti = 0.0;
             cmac(tr, ti, a, xr);
             atomicAdd(&y[c].x, tr);
             atomicAdd(&y[c].y, ti);
+        }
+    };
+    // two consecutive entries per lane and step: the column pair is one
+    // 16-byte load, so a warp moves 512 B of columns and 1 KiB of values per
+    // step with three load instructions.  idx is 8-byte aligned (checked on
+    // the host); a leading entry at an address that is not 16-byte aligned
+    // is taken first
+    int64_t jb = j0;
+    if ((reinterpret_cast<uintptr_t>(idx + jb) & 15) && jb < j1) {
+        if (lane == 0) entry(idx[jb], A[jb]);
+        ++jb;
+    }
+#pragma unroll 4
+    for (int64_t j = jb + 2 * lane; j < j1; j += 64) {
+        if (j + 1 < j1) {
+            const longlong2 cc = *reinterpret_cast<const longlong2 *>(idx + j);
+            const double2 a0 = A[j], a1 = A[j + 1];
+            entry(cc.x, a0);
+            entry(cc.y, a1);
+        } else {
+            entry(idx[j], A[j]);
         }
     }
     if (OP == 1) return;

@@ -205,3 +205,30 @@ def test_misaligned_device_pointers_rejected(bs2e):
         ok = dict(shape=(1, 1), nnz=1, index_ptr=np.array([1, 2]), indices=np.array([1]),
                   data=np.array([2.0 + 0j]))
         np.testing.assert_allclose(h.csr_mv(ok, np.array([3.0 + 0j])), [6.0])
+
+
+@pytest.mark.gpu
+def test_gpu_mv_columns_8_byte_aligned(bs2e, oracle):
+    """Column indices that start 8 bytes past a 16-byte boundary (valid: int64
+    arrays need 8-byte alignment) take the vector path after one leading
+    entry per row where needed; rows of every parity of start and length."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    A = _random_csr(rng, 200, 150, 0.07)
+    x = rng.standard_normal(150) + 1j * rng.standard_normal(150)
+    want, scale = oracle.csr_mv(0, A["shape"], A["index_ptr"], A["indices"], A["data"], x)
+    dev = torch.device("cuda", 0)
+    c = CASES["cfg1"]
+    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+        for shift in (0, 1):
+            idx_buf = torch.zeros(A["nnz"] + 1, dtype=torch.int64, device=dev)
+            idx = idx_buf[shift:shift + A["nnz"]]
+            idx.copy_(torch.from_numpy(A["indices"]))
+            assert (idx.data_ptr() % 16 == 0) == (shift == 0)
+            ptr = torch.from_numpy(A["index_ptr"]).to(dev)
+            dat = torch.from_numpy(A["data"]).to(dev)
+            xd = torch.from_numpy(x).to(dev)
+            yd = torch.empty(200, dtype=torch.complex128, device=dev)
+            h.csr_mv_device(0, 200, 150, A["nnz"], ptr.data_ptr(), idx.data_ptr(),
+                            dat.data_ptr(), xd.data_ptr(), yd.data_ptr())
+            _check(yd.cpu().numpy(), want, scale)
