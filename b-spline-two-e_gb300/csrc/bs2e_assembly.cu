@@ -543,6 +543,21 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
         const double *ax = ad + K1;
         int Ed = 0, Ex = 0;
         bool wide = false;
+        // FP64: this pair's weights and multipole tile offsets in the warp's
+        // shared scratch (the FP32-pair slots), read as broadcasts in the sums
+        double (*sAd)[kMaxK1] = reinterpret_cast<double (*)[kMaxK1]>(sAw);
+        if (!MIXED) {
+            __syncwarp();  // every lane is done with the previous pair's values
+            if (lane < pi.nd) {
+                sAd[0][lane] = ad[lane];
+                sKow[0][lane] = kd[lane] * W2;
+            }
+            if (lane < pi.nx) {
+                sAd[1][lane] = ax[lane];
+                sKow[1][lane] = kx[lane] * W2;
+            }
+            __syncwarp();
+        }
         if (MIXED) {
             // scaled multipole weights of this channel pair for this tile
             int ed = -100000, ex = -100000;
@@ -709,11 +724,11 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                 double rd = 0.0, rx = 0.0;
                                 if (sup) {
                                     const double *Rt = sR + od;
-                                    for (int u = 0; u < pi.nd; ++u) rd = fma(Rt[kd[u] * W2], ad[u], rd);
+                                    for (int u = 0; u < pi.nd; ++u) rd = fma(Rt[sKow[0][u]], sAd[0][u], rd);
                                 }
                                 if (supx) {
                                     const double *Rt = sR + ox;
-                                    for (int u = 0; u < pi.nx; ++u) rx = fma(Rt[kx[u] * W2], ax[u], rx);
+                                    for (int u = 0; u < pi.nx; ++u) rx = fma(Rt[sKow[1][u]], sAd[1][u], rx);
                                 }
                                 re = (sup && supx) ? rd + rx : (sup ? rd : rx);
                             }
