@@ -467,7 +467,8 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
 }
 
 // Minimum resident CTAs per SM the fill kernel is compiled for (caps its
-// registers at 65536 / (128 * this)).  Measured on config 2 (fill time per
+// registers at 65536 / (128 * this)).  Measured on the order-7, N=200,
+// k=0..10, l_max=5, L=0..3 singlet+triplet workload (fill time per
 // step, FP64 / mixed): 8 -> 39.2 / 42.7 ms (64 registers), 6 -> 40.3 / 45.9,
 // 4 -> 46.8 / 50.7; the kernel is bound by the FP64 pipe (plain) and the
 // integer ALU pipe (mixed), not by occupancy.

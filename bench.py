@@ -15,7 +15,7 @@ roofline: the CSR fill kernel (k_csr_fill), timed with CUDA events on the
         library's stream; algorithmic bytes = 24 B per stored H/S entry
         (int64 index + complex128 value) + the R^k tiles it stages.  traffic:
         DRAM bytes per launch, from the ncu capture of block 0 (profiles/
-        k_csr_fill_config2_block0.md) scaled to the average launch by
+        k_csr_fill_order7_n200_block0.md) scaled to the average launch by
         algorithmic bytes.
 cpu_baseline: the CPU oracle (C restatement of the reference, OpenMP) on a
         bounded sample: full Slater primitives + R^k map, and a row sample of
@@ -31,6 +31,12 @@ python bench.py --workload batch    the ragged batch of 64 radial problems
                                     (tests/golden/ragged_problems.json): batched,
                                     graph-captured radial stage vs the same 64
                                     problems one handle after another
+python bench.py --workload matvec   CSR mat-vec over the singlet H blocks of the
+                                    default workload, assembled into HBM
+python bench.py --workload order9_n800
+                                    order 9, N=800, r_max=800, q=12, k=0..20,
+                                    l_max=10, singlet L=0..5: radial stage, block
+                                    counts and row samples of every block
 """
 import argparse
 import json
@@ -50,7 +56,7 @@ WORKLOAD = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5, max_L=3, Z=2
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of the k_csr_fill launch on
-# block 0 (ncu --set full, profiles/k_csr_fill_config2_block0.md) and that
+# block 0 (ncu --set full, profiles/k_csr_fill_order7_n200_block0.md) and that
 # launch's algorithmic bytes (3,154,438,224 B of CSR + 20,100 staged tiles).
 NCU_BLOCK0_DRAM = {"fp64": 3563240624.0, "mixed": 3518698768.0}
 NCU_BLOCK0_ALG = 3453526224.0
@@ -499,11 +505,11 @@ def run_batch(args):
     }
 
 
-CONFIG5 = dict(k=9, n_b=800, r_max=800.0, q=12, max_k=20, l_max=10, max_L=5, Z=2, cap_order=2,
+LARGE = dict(k=9, n_b=800, r_max=800.0, q=12, max_k=20, l_max=10, max_L=5, Z=2, cap_order=2,
                cap_r0=10.0, cap_eta=1e-3)
 
 
-def run_config5(args, sample_rows=2048):
+def run_large(args, sample_rows=2048):
     """The large configuration (order 9, N=800, r_max=800, 12 GL points,
     k=0..20, l_max=10, singlet L=0..5 with the L+-1 dipole blocks, q=0).  Its
     CSR (terabytes) exceeds HBM and host memory, so: the radial stage and the
@@ -513,7 +519,7 @@ def run_config5(args, sample_rows=2048):
     compared with the FP64 path on the same samples."""
     import torch
     pkg = _pkg()
-    w = CONFIG5
+    w = LARGE
     dev = torch.device("cuda", 0)
     t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
     syms = pkg.basis.symmetries(w["max_L"], True)
@@ -550,6 +556,7 @@ def run_config5(args, sample_rows=2048):
     blocks = []
     tot_s = {"fp64": 0.0, "mixed": 0.0}
     worst = 0.0
+    worst_max = 0.0
     for (L, M, par, cf) in cfs:
         n = cf.size
         b = {"L": L, "rows": int(n)}
@@ -596,23 +603,36 @@ def run_config5(args, sample_rows=2048):
             b["assembly_s_extrapolated_" + name] = (nH + nS) / rate
             tot_s[name] += (nH + nS) / rate
         same = True
-        rel = 0.0
+        rel = 0.0  # |mixed - fp64| / |fp64| over entries >= 1e-10 of the sample's largest
+        rel_max = 0.0  # |mixed - fp64| / largest |fp64| of the sample range
         for (i1, d1, si1, sd1), (i2, d2, si2, sd2) in zip(samples["fp64"], samples["mixed"]):
             same = same and torch.equal(i1, i2) and torch.equal(si1, si2)
             for x, y in ((d1, d2), (sd1, sd2)):
                 ax = x.abs()
-                mask = ax >= 1e-10 * float(ax.max())
+                if ax.numel() == 0:
+                    continue
+                top = float(ax.max())
+                mask = ax >= 1e-10 * top
                 if mask.any():
                     rel = max(rel, float(((y - x).abs()[mask] / ax[mask]).max()))
+                if top > 0:
+                    rel_max = max(rel_max, float((y - x).abs().max()) / top)
         b["pattern_identical_mixed_vs_fp64"] = bool(same)
-        b["max_rel_err_mixed_vs_fp64"] = rel
+        b["max_err_rel_to_entry_mixed_vs_fp64"] = rel
+        b["max_err_rel_to_sample_max_mixed_vs_fp64"] = rel_max
         worst = max(worst, rel)
+        worst_max = max(worst_max, rel_max)
         blocks.append(b)
         torch.cuda.empty_cache()
     out["blocks"] = blocks
     out["assembly_s_extrapolated_fp64"] = tot_s["fp64"]
     out["assembly_s_extrapolated_mixed"] = tot_s["mixed"]
-    out["max_rel_err_mixed_vs_fp64"] = worst
+    # Relative to the entry, a value that cancels between the multipole terms
+    # shows the terms' rounding magnified; the 1e-9 bar is relative to the
+    # term magnitude, which tests/test_precision_report.py checks against the
+    # oracle on these blocks.
+    out["max_err_rel_to_entry_mixed_vs_fp64"] = worst
+    out["max_err_rel_to_sample_max_mixed_vs_fp64"] = worst_max
     # dipole blocks L -> L+1, q = 0 (z polarisation), length gauge
     h = hs["fp64"][0]
     h.radial_dipole(0, copy_out=False)
@@ -753,8 +773,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-block", type=int, default=None)
-    ap.add_argument("--workload", default="config2",
-                    choices=["config2", "batch", "matvec", "config5"])
+    ap.add_argument("--workload", default="order7_n200",
+                    choices=["order7_n200", "batch", "matvec", "order9_n800"])
     args = ap.parse_args()
     if args.profile_block is not None:
         profile_block(args)
@@ -765,8 +785,8 @@ def main():
     if args.workload == "matvec":
         print(json.dumps(run_matvec(args)), flush=True)
         return
-    if args.workload == "config5":
-        print(json.dumps(run_config5(args)), flush=True)
+    if args.workload == "order9_n800":
+        print(json.dumps(run_large(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

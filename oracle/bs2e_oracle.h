@@ -2,8 +2,8 @@
  * bs2e_oracle.h -- CPU oracle for the two-electron matrix-element path.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
- * Fortran (edvinolo/b-spline-two-e, src/mat_els + src/tools) used as the
- * parity checker and as the timed CPU baseline.  Only tests/, the smoke check
+ * Fortran (edvinolo/b-spline-two-e, src/mat_els + src/tools) that the parity
+ * tests compare the GPU library with, and the timed CPU baseline.  Only tests/, the smoke check
  * and the CPU-baseline leg of bench.py may load it.  The GPU library never
  * links or calls anything here.
  *

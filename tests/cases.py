@@ -1,8 +1,8 @@
 """Test cases shared by the CPU and GPU suites.
 
-cfg1 is the reference-sized CPU case (k=6, 60 B-splines on the exp-linear grid
+ref60 is the reference-sized CPU case (k=6, 60 B-splines on the exp-linear grid
 to r_max=50, 8 GL points, k=0..4, singlet L=0 with l1=l2 in {0,1,2}).  small2
-is config 2's method (k=7, 10 GL points, k=0..10, l_max=5, L=0..3, singlet and
+is the order-7 N=200 workload's method (k=7, 10 GL points, k=0..10, l_max=5, L=0..3, singlet and
 triplet) on 30 B-splines so the O(n_config^2) oracle finishes in seconds.  cut
 exercises the r_2_max / r_all_l / max_l2 cuts and the non-z-polarised
 (unnatural parity) symmetry list.
@@ -12,7 +12,7 @@ import functools
 import numpy as np
 
 CASES = {
-    "cfg1": dict(k=6, n_b=60, r_max=50.0, q=8, max_k=4, lmax=2, max_L=0, z_pol=True,
+    "ref60": dict(k=6, n_b=60, r_max=50.0, q=8, max_k=4, lmax=2, max_L=0, z_pol=True,
                  spins=(0,), Z=2),
     "small2": dict(k=7, n_b=30, r_max=30.0, q=10, max_k=10, lmax=5, max_L=3, z_pol=True,
                    spins=(0, 1), Z=2),

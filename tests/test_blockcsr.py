@@ -62,8 +62,8 @@ def test_gpu_join_matches_oracle(bs2e, oracle):
     rows, cols, dens = GRID
     G = _grid(rng, rows, cols, dens)
     want = oracle.csr_from_blocks(G, len(rows), len(cols))
-    c = CASES["cfg1"]
-    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
         got = h.csr_from_blocks(G, len(rows), len(cols))
     for key in ("index_ptr", "indices", "data"):
         np.testing.assert_array_equal(got[key], want[key])
@@ -111,8 +111,8 @@ def test_gpu_join_symmetry_and_dipole_blocks(bs2e, oracle):
 
 @pytest.mark.gpu
 def test_gpu_join_errors(bs2e):
-    c = CASES["cfg1"]
-    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
         bad = {(0, 0): dict(shape=(2, 2), nnz=2, index_ptr=np.array([1, 5, 3]),
                             indices=np.array([1, 2]), data=np.ones(2, np.complex128))}
         with pytest.raises(bs2e.Bs2eError, match="index_ptr"):

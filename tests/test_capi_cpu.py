@@ -74,7 +74,7 @@ def test_explin_knots_sizes(bs2e):
         assert (t[:k] == 0).all() and (t[-k:] == rmax).all()
         n_iv = np.unique(t).size - 1
         assert n_iv == t.size - 2 * k + 1
-    # cfg1 has 57 breakpoint intervals (survey 8(d))
+    # order 6, 60 B-splines to r_max=50 has 57 breakpoint intervals
     assert np.unique(bs2e.grids.explin_knots(6, 60, 50.0)).size - 1 == 57
 
 

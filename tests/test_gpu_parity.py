@@ -21,7 +21,7 @@ def _handle(bs2e, case, precision=0):
     return h
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "cut"])
+@pytest.mark.parametrize("case", ["ref60", "small2", "cut"])
 def test_primitives_match_oracle(bs2e, oracle, case):
     ref = oracle_reference(case)["prim"]
     with _handle(bs2e, case) as h:
@@ -33,7 +33,7 @@ def test_primitives_match_oracle(bs2e, oracle, case):
         np.testing.assert_allclose(g[name], ref[name], rtol=1e-13, atol=0, err_msg=name)
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "cut"])
+@pytest.mark.parametrize("case", ["ref60", "small2", "cut"])
 def test_rk_store_matches_oracle(bs2e, oracle, case):
     c = CASES[case]
     R = oracle_reference(case)["R"]
@@ -62,7 +62,7 @@ def test_rk_partial_multipole_range(bs2e, oracle):
     np.testing.assert_allclose(got, oracle.rk_lookup(R, c["k"], keys), rtol=RTOL)
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2"])
+@pytest.mark.parametrize("case", ["ref60", "small2"])
 def test_one_body_matches_oracle(bs2e, oracle, case):
     c = CASES[case]
     ref = oracle_reference(case)
@@ -74,7 +74,7 @@ def test_one_body_matches_oracle(bs2e, oracle, case):
         np.testing.assert_allclose(H[:, :, l], ref["H1p"][:, :, l], rtol=0, atol=1e-12 * scale)
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "cut"])
+@pytest.mark.parametrize("case", ["ref60", "small2", "cut"])
 @pytest.mark.parametrize("full", [True, False])
 def test_blocks_match_oracle(bs2e, oracle, case, full):
     c = CASES[case]
@@ -118,9 +118,9 @@ def test_device_outputs_match_host_outputs(bs2e, oracle):
 
 
 def test_empty_block_and_error_paths(bs2e, oracle):
-    c = CASES["cfg1"]
-    ref = oracle_reference("cfg1")
-    with _handle(bs2e, "cfg1") as h:
+    c = CASES["ref60"]
+    ref = oracle_reference("ref60")
+    with _handle(bs2e, "ref60") as h:
         cf = np.zeros(0, dtype=bs2e.CONFIG_DTYPE)
         with pytest.raises(bs2e.Bs2eError) as e:  # R^k not built yet
             h.block(cf, 0)
@@ -129,7 +129,7 @@ def test_empty_block_and_error_paths(bs2e, oracle):
         h.set_one_body(ref["H1p"], ref["S"])
         H, S = h.block(cf, 0)
         assert H["nnz"] == 0 and list(H["index_ptr"]) == [1]
-        good = blocks(bs2e, "cfg1")[0][4]
+        good = blocks(bs2e, "ref60")[0][4]
         bad = np.concatenate([good[good["l1"] == 1], good[good["l1"] == 0]])
         bad = np.concatenate([bad, good[good["l1"] == 1][:1]])  # channel (1,1) split in two
         with pytest.raises(bs2e.Bs2eError) as e:
@@ -172,7 +172,7 @@ def test_gpu_hydrogenic_known_answer(bs2e, oracle):
 MIXED_RTOL = 1e-11
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "wide"])
+@pytest.mark.parametrize("case", ["ref60", "small2", "wide"])
 def test_mixed_rk_store_matches_oracle(bs2e, oracle, case):
     c = CASES[case]
     R = oracle_reference(case)["R"]
@@ -188,7 +188,7 @@ def test_mixed_rk_store_matches_oracle(bs2e, oracle, case):
     np.testing.assert_allclose(got, oracle.rk_lookup(R, k, keys), rtol=1e-13, atol=0)
 
 
-@pytest.mark.parametrize("case", ["cfg1", "small2", "cut", "wide"])
+@pytest.mark.parametrize("case", ["ref60", "small2", "cut", "wide"])
 def test_mixed_blocks_match_oracle(bs2e, oracle, case):
     c = CASES[case]
     ref = oracle_reference(case)

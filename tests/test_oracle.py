@@ -46,14 +46,15 @@ def test_wigner_vs_golden(oracle):
 
 
 def test_configs_match_reference_counts(oracle, bs2e):
-    # cfg1 row count of the survey, and the config-2 block sizes
+    # rows of the order-6 N=60 l_max=2 singlet L=0 block, and the block sizes of
+    # order 7, N=200, l_max=5, L=0..3
     assert oracle.count_configs(0, 0, 2, 60, 6).size == 5311
     for (L, par), n in {(0, 0): 117620, (1, 1): 195040, (2, 0): 253546, (3, 1): 272254}.items():
         assert oracle.count_configs(L, par, 5, 200, 7).size == n
 
 
 def test_count_nnz_equals_construct(oracle, bs2e):
-    for case in ("cfg1", "small2", "cut"):
+    for case in ("ref60", "small2", "cut"):
         c = CASES[case]
         ref = oracle_reference(case)
         for (L, M, par, spin, cf) in blocks(bs2e, case):
@@ -114,8 +115,8 @@ def test_hydrogenic_slater_integrals(oracle):
 
 
 def test_rk_symmetries_and_positivity(oracle, bs2e):
-    c = CASES["cfg1"]
-    R = oracle_reference("cfg1")["R"]
+    c = CASES["ref60"]
+    R = oracle_reference("ref60")["R"]
     k, N = c["k"], c["n_b"]
     rng = np.random.default_rng(3)
     keys = []

@@ -122,8 +122,8 @@ def test_gpu_mv_random_and_rectangular(bs2e, oracle, op):
     n_in = shape[0] if op == 1 else shape[1]
     x = rng.standard_normal(n_in) + 1j * rng.standard_normal(n_in)
     want, scale = oracle.csr_mv(op, A["shape"], A["index_ptr"], A["indices"], A["data"], x)
-    c = CASES["cfg1"]
-    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
         _check(h.csr_mv(A, x, op), want, scale)
 
 
@@ -165,8 +165,8 @@ def test_gpu_mv_on_device_blocks(bs2e, oracle):
 
 @pytest.mark.gpu
 def test_gpu_mv_empty_and_errors(bs2e):
-    c = CASES["cfg1"]
-    t = oracle_reference("cfg1")["knots"]
+    c = CASES["ref60"]
+    t = oracle_reference("ref60")["knots"]
     with bs2e.Bs2e(t, c["k"], c["q"], c["max_k"]) as h:
         E = dict(shape=(4, 3), nnz=0, index_ptr=np.ones(5, np.int64), indices=None, data=None)
         for op in (0, 1):
@@ -194,11 +194,11 @@ def test_misaligned_device_pointers_rejected(bs2e):
     """Device pointers that break the 8/16-byte alignment of int64 / complex128
     arrays are refused on the host before any kernel runs."""
     torch = pytest.importorskip("torch")
-    c = CASES["cfg1"]
+    c = CASES["ref60"]
     dev = torch.device("cuda", 0)
     raw = torch.zeros(64, dtype=torch.float64, device=dev)
     p = raw.data_ptr()
-    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
         with pytest.raises(bs2e.Bs2eError, match="align"):
             h.csr_mv_device(0, 2, 2, 2, p, p + 24, p + 8 * 9, p + 8 * 20, p + 8 * 30)
         # the handle stays usable
@@ -218,8 +218,8 @@ def test_gpu_mv_columns_8_byte_aligned(bs2e, oracle):
     x = rng.standard_normal(150) + 1j * rng.standard_normal(150)
     want, scale = oracle.csr_mv(0, A["shape"], A["index_ptr"], A["indices"], A["data"], x)
     dev = torch.device("cuda", 0)
-    c = CASES["cfg1"]
-    with bs2e.Bs2e(oracle_reference("cfg1")["knots"], c["k"], c["q"], c["max_k"]) as h:
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
         for shift in (0, 1):
             idx_buf = torch.zeros(A["nnz"] + 1, dtype=torch.int64, device=dev)
             idx = idx_buf[shift:shift + A["nnz"]]
