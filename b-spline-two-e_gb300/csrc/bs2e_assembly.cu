@@ -385,6 +385,12 @@ __device__ __forceinline__ void ff_madd(FF &acc, float2 a, float2 x) {
     acc.c = __fadd_rn(acc.c, __fadd_rn(err, e));
 }
 
+// x with its sign bit flipped when bit is the sign bit: multiplication by an
+// exchange sign of +-1 as one integer operation instead of an FP64 one.
+__device__ __forceinline__ double flip_sign(double x, long long bit) {
+    return __longlong_as_double(__double_as_longlong(x) ^ bit);
+}
+
 // 2^n as float for -126 <= n <= 127, 0 below.
 __device__ __forceinline__ float pow2f(int n) {
     return n < -126 ? 0.0f : __int_as_float((127 + min(n, 127)) << 23);
@@ -467,13 +473,17 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
 }
 
 // Minimum resident CTAs per SM the fill kernel is compiled for (caps its
-// registers at 65536 / (128 * this)).  Measured on the order-7, N=200,
-// k=0..10, l_max=5, L=0..3 singlet+triplet workload (fill time per
-// step, FP64 / mixed): 8 -> 39.2 / 42.7 ms (64 registers), 6 -> 40.3 / 45.9,
-// 4 -> 46.8 / 50.7; the kernel is bound by the FP64 pipe (plain) and the
-// integer ALU pipe (mixed), not by occupancy.
+// registers at 65536 / (128 * this)), for the mixed and the FP64 kernel.
+// Measured on the order-7, N=200, k=0..10, l_max=5, L=0..3 singlet+triplet
+// workload (fill time per step): mixed 8 -> 42.7 ms (64 registers), 6 ->
+// 45.9, 4 -> 50.7; FP64 8 -> 28.3 ms, 6 -> 32.1 (80 registers), 10 -> 35.8
+// (48, spilling), 12 -> 40.5.  Fewer registers spill in the entry loop, more
+// leave too few warps to hide the FP64 and shuffle latencies.
 #ifndef BS2E_FILL_MIN_BLOCKS
 #define BS2E_FILL_MIN_BLOCKS 8
+#endif
+#ifndef BS2E_FILL_MIN_BLOCKS_FP64
+#define BS2E_FILL_MIN_BLOCKS_FP64 8
 #endif
 
 // Direct + exchange multipole sums of one entry in FP64 from the mixed store
@@ -526,6 +536,9 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
     const float4 *HbB = F.Hbf ? F.Hbf + (size_t)l_b * A.N * W + rb : nullptr;  // H_lb[n_b][.]
     const float4 *SA = F.Sbf ? F.Sbf + ra : nullptr;                           // S[n_a][.]
     const float4 *SB = F.Sbf ? F.Sbf + rb : nullptr;                           // S[n_b][.]
+    const double2 *HaR = F.Hb + (size_t)l_a * A.N * W + ra;  // FP64 band rows, same indexing
+    const double2 *HbR = F.Hb + (size_t)l_b * A.N * W + rb;
+    const double2 *SaR = F.Sb + ra, *SbR = F.Sb + rb;
     int64_t oH = F.Hptr[row - F.ptr_row0] - 1 - F.Hbase;
     int64_t oS = F.Sptr[row - F.ptr_row0] - 1 - F.Sbase;
     for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
@@ -534,6 +547,8 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
         const bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
         const bool Aok = dir_ok || leq || leqx, Bok = ex_ok || leq || leqx;
         if (!Aok && !Bok) continue;
+        // the exchange sign (+-1) as a sign bit
+        const long long sgn_bit = __double_as_longlong(pi.sgn) & (long long)0x8000000000000000ULL;
         const int nlo = (!A.full && c_c == c_r) ? n_a : 1;
         const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, Aok, Bok, nlo);
         const int ncand = cand.l1 + cand.l2;
@@ -677,7 +692,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                     const int dc = n_d - n_a, dd = r_nc - n_b;
                                     float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
                                     float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
-                                    bool ng = pi.sgn < 0.0;
+                                    const bool ng = sgn_bit != 0;
                                     FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
                                                    ff_mul(make_float2(h2.x, h2.y), s2r));
                                     FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
@@ -720,42 +735,43 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                 FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
                                 re = ff_to_double(v, Ev - kRkBias);
                             } else {
-                                // direct and exchange multipole sums; the add joining
-                                // them runs only where both are present
-                                double rd = 0.0, rx = 0.0;
+                                // direct and exchange multipole sums in one accumulator
+                                // (no FP64 add joins them)
                                 if (sup) {
                                     const double *Rt = sR + od;
-                                    for (int u = 0; u < pi.nd; ++u) rd = fma(Rt[sKow[0][u]], sAd[0][u], rd);
+                                    for (int u = 0; u < pi.nd; ++u) re = fma(Rt[sKow[0][u]], sAd[0][u], re);
                                 }
                                 if (supx) {
                                     const double *Rt = sR + ox;
-                                    for (int u = 0; u < pi.nx; ++u) rx = fma(Rt[sKow[1][u]], sAd[1][u], rx);
+                                    for (int u = 0; u < pi.nx; ++u) re = fma(Rt[sKow[1][u]], sAd[1][u], re);
                                 }
-                                re = (sup && supx) ? rd + rx : (sup ? rd : rx);
                             }
                         }
                         if (one && !(MIXED && F.ff_one_body) && F.s_real) {
                             // H_1p_neq (mat_els.f90:697-715) with a real S: the l_eq
                             // term is non-zero only under sup, the l_eq_ex term only
-                            // under sup_x (both lookups inside the band)
-                            const int N = A.N;
-                            const double2 *Ha = F.Hb + (size_t)l_a * N * W;
-                            const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
-                            double hr = 0.0, hi = 0.0;
+                            // under sup_x (both lookups inside the band); its
+                            // products go straight into the entry's accumulators
+                            // and the exchange sign flips the S factors
                             if (leq && sup) {
-                                const double2 h1 = band(Ha, N, k, n_a, r_nc), h2 = band(Hbb, N, k, n_b, n_d);
-                                const double s1 = band(F.Sb, N, k, n_b, n_d).x, s2 = band(F.Sb, N, k, n_a, r_nc).x;
-                                hr = fma(h1.x, s1, h2.x * s2);
-                                hi = fma(h1.y, s1, h2.y * s2);
+                                const int dc = r_nc - n_a, dd = n_d - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+                                re = fma(h1.x, s1, re);
+                                re = fma(h2.x, s2, re);
+                                im = fma(h1.y, s1, im);
+                                im = fma(h2.y, s2, im);
                             }
                             if (leqx && supx) {
-                                const double2 h1 = band(Ha, N, k, n_a, n_d), h2 = band(Hbb, N, k, n_b, r_nc);
-                                const double s1 = band(F.Sb, N, k, n_b, r_nc).x, s2 = band(F.Sb, N, k, n_a, n_d).x;
-                                hr = fma(pi.sgn, fma(h1.x, s1, h2.x * s2), hr);
-                                hi = fma(pi.sgn, fma(h1.y, s1, h2.y * s2), hi);
+                                const int dc = n_d - n_a, dd = r_nc - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = flip_sign(SbR[dd].x, sgn_bit);
+                                const double s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                re = fma(h1.x, s1, re);
+                                re = fma(h2.x, s2, re);
+                                im = fma(h1.y, s1, im);
+                                im = fma(h2.y, s2, im);
                             }
-                            re = re + hr;
-                            im = im + hi;
                         } else if (one && !(MIXED && F.ff_one_body)) {
                             // H_1p_neq (mat_els.f90:697-715), complex S
                             const int N = A.N;
@@ -826,7 +842,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                             if (leqx && supx) {
                                 float4 a = SA[n_d - n_a], b = SB[r_nc - n_b];
                                 t = ff_add(t, ff_neg_if(ff_mul(make_float2(a.x, a.y), make_float2(b.x, b.y)),
-                                                        pi.sgn < 0.0));
+                                                        sgn_bit != 0));
                             }
                             s1 = make_double2(ff_to_double(t, 0), 0.0);
                         } else if (F.s_real) {
@@ -834,9 +850,9 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                             const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
                             const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
                             double sr = 0.0;
-                            if (leq && sup) sr = band(F.Sb, N, k, n_a, r_nc).x * band(F.Sb, N, k, n_b, n_d).x;
+                            if (leq && sup) sr = SaR[r_nc - n_a].x * SbR[n_d - n_b].x;
                             if (leqx && supx)
-                                sr = fma(pi.sgn * band(F.Sb, N, k, n_a, n_d).x, band(F.Sb, N, k, n_b, r_nc).x, sr);
+                                sr = fma(flip_sign(SaR[n_d - n_a].x, sgn_bit), SbR[r_nc - n_b].x, sr);
                             s1 = make_double2(sr, 0.0);
                         } else {
                             if (leq) s1 = cadd(s1, cmul(band(F.Sb, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d)));
@@ -857,7 +873,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
 }
 
 template <bool MIXED>
-__global__ void __launch_bounds__(128, BS2E_FILL_MIN_BLOCKS) k_csr_fill(FillArgs F) {
+__global__ void __launch_bounds__(128, MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
     __shared__ int sexp[kMaxK1];
