@@ -626,174 +626,281 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                 }
                 const int excl = incl - cnt;
                 const int tot = __shfl_sync(FULL, incl, 31);
-                for (int e0 = 0; e0 < tot; e0 += 32) {
-                    const int e = e0 + lane;
-                    int pos = 0;
+                if (!MIXED && F.s_real) {
+                    // FP64 with a real S: two entries per lane (e and e + 32 of
+                    // each 64), so the two run searches and the two multipole
+                    // FMA chains are independent and overlap; an entry outside
+                    // sup (sup_x) reads a valid tile element and drops the sum
+                    for (int e0 = 0; e0 < tot; e0 += 64) {
+                        const int eA = e0 + lane, eB = eA + 32;
+                        int pA = 0, pB = 0;
 #pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        int cand_pos = pos + step;
-                        int v = __shfl_sync(FULL, excl, cand_pos);
-                        if (v <= e) pos = cand_pos;
+                        for (int step = 16; step > 0; step >>= 1) {
+                            const int vA = __shfl_sync(FULL, excl, pA + step);
+                            const int vB = __shfl_sync(FULL, excl, pB + step);
+                            if (vA <= eA) pA += step;
+                            if (vB <= eB) pB += step;
+                        }
+                        int ncA, ndA, jA, ncB, ndB, jB;
+                        {
+                            const int o = eA - __shfl_sync(FULL, excl, pA);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pA);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pA), s2 = __shfl_sync(FULL, hs.s2, pA);
+                            ncA = __shfl_sync(FULL, n_c, pA);
+                            ndA = o < l1 ? s1 + o : s2 + (o - l1);
+                            jA = __shfl_sync(FULL, base, pA) + (ndA - __shfl_sync(FULL, lo, pA));
+                        }
+                        {
+                            const int o = eB - __shfl_sync(FULL, excl, pB);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pB);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pB), s2 = __shfl_sync(FULL, hs.s2, pB);
+                            ncB = __shfl_sync(FULL, n_c, pB);
+                            ndB = o < l1 ? s1 + o : s2 + (o - l1);
+                            jB = __shfl_sync(FULL, base, pB) + (ndB - __shfl_sync(FULL, lo, pB));
+                        }
+                        const bool liveA = eA < tot, liveB = eB < tot;
+                        const bool supA = liveA && abs(n_a - ncA) < k && abs(n_b - ndA) < k;
+                        const bool supxA = liveA && abs(n_a - ndA) < k && abs(n_b - ncA) < k;
+                        const bool supB = liveB && abs(n_a - ncB) < k && abs(n_b - ndB) < k;
+                        const bool supxB = liveB && abs(n_a - ndB) < k && abs(n_b - ncB) < k;
+                        double reA = 0.0, imA = 0.0, reB = 0.0, imB = 0.0;
+                        if (supA || supB) {
+                            const int oA = supA ? (ncA - n_a + k - 1) * W + (ndA - n_b + k - 1) : 0;
+                            const int oB = supB ? (ncB - n_a + k - 1) * W + (ndB - n_b + k - 1) : 0;
+                            double a = 0.0, b = 0.0;
+                            for (int u = 0; u < pi.nd; ++u) {
+                                const int ko = sKow[0][u];
+                                const double w = sAd[0][u];
+                                a = fma(sR[oA + ko], w, a);
+                                b = fma(sR[oB + ko], w, b);
+                            }
+                            reA = supA ? a : 0.0;
+                            reB = supB ? b : 0.0;
+                        }
+                        if (supxA || supxB) {
+                            const int oA = supxA ? (ndA - n_a + k - 1) * W + (ncA - n_b + k - 1) : 0;
+                            const int oB = supxB ? (ndB - n_a + k - 1) * W + (ncB - n_b + k - 1) : 0;
+                            double a = reA, b = reB;
+                            for (int u = 0; u < pi.nx; ++u) {
+                                const int ko = sKow[1][u];
+                                const double w = sAd[1][u];
+                                a = fma(sR[oA + ko], w, a);
+                                b = fma(sR[oB + ko], w, b);
+                            }
+                            reA = supxA ? a : reA;
+                            reB = supxB ? b : reB;
+                        }
+                        if (leq && (supA || supB)) {
+                            const int dcA = supA ? ncA - n_a : 0, ddA = supA ? ndA - n_b : 0;
+                            const int dcB = supB ? ncB - n_a : 0, ddB = supB ? ndB - n_b : 0;
+                            const double2 h1A = HaR[dcA], h2A = HbR[ddA], h1B = HaR[dcB], h2B = HbR[ddB];
+                            const double s1A = supA ? SbR[ddA].x : 0.0, s2A = supA ? SaR[dcA].x : 0.0;
+                            const double s1B = supB ? SbR[ddB].x : 0.0, s2B = supB ? SaR[dcB].x : 0.0;
+                            reA = fma(h1A.x, s1A, reA);
+                            reB = fma(h1B.x, s1B, reB);
+                            reA = fma(h2A.x, s2A, reA);
+                            reB = fma(h2B.x, s2B, reB);
+                            imA = fma(h1A.y, s1A, imA);
+                            imB = fma(h1B.y, s1B, imB);
+                            imA = fma(h2A.y, s2A, imA);
+                            imB = fma(h2B.y, s2B, imB);
+                        }
+                        if (leqx && (supxA || supxB)) {
+                            const int dcA = supxA ? ndA - n_a : 0, ddA = supxA ? ncA - n_b : 0;
+                            const int dcB = supxB ? ndB - n_a : 0, ddB = supxB ? ncB - n_b : 0;
+                            const double2 h1A = HaR[dcA], h2A = HbR[ddA], h1B = HaR[dcB], h2B = HbR[ddB];
+                            const double s1A = supxA ? flip_sign(SbR[ddA].x, sgn_bit) : 0.0;
+                            const double s2A = supxA ? flip_sign(SaR[dcA].x, sgn_bit) : 0.0;
+                            const double s1B = supxB ? flip_sign(SbR[ddB].x, sgn_bit) : 0.0;
+                            const double s2B = supxB ? flip_sign(SaR[dcB].x, sgn_bit) : 0.0;
+                            reA = fma(h1A.x, s1A, reA);
+                            reB = fma(h1B.x, s1B, reB);
+                            reA = fma(h2A.x, s2A, reA);
+                            reB = fma(h2B.x, s2B, reB);
+                            imA = fma(h1A.y, s1A, imA);
+                            imB = fma(h1B.y, s1B, imB);
+                            imA = fma(h2A.y, s2A, imA);
+                            imB = fma(h2B.y, s2B, imB);
+                        }
+                        if (liveA) {
+                            F.Hidx[oH + eA] = (int64_t)jA + 1;
+                            F.Hdat[oH + eA] = make_double2(reA, imA);
+                        }
+                        if (liveB) {
+                            F.Hidx[oH + eB] = (int64_t)jB + 1;
+                            F.Hdat[oH + eB] = make_double2(reB, imB);
+                        }
                     }
-                    const int o_ex = __shfl_sync(FULL, excl, pos);
-                    const int r_nc = __shfl_sync(FULL, n_c, pos);
-                    const int r_base = __shfl_sync(FULL, base, pos);
-                    const int r_lo = __shfl_sync(FULL, lo, pos);
-                    const int r_s1 = __shfl_sync(FULL, hs.s1, pos);
-                    const int r_l1 = __shfl_sync(FULL, hs.l1, pos);
-                    const int r_s2 = __shfl_sync(FULL, hs.s2, pos);
-                    if (e < tot) {
-                        const int o = e - o_ex;
-                        const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
-                        const int j = r_base + (n_d - r_lo);
-                        const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
-                        const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
-                        double re = 0.0, im = 0.0;
-                        const bool r12 = (sup && dir_ok) || (supx && ex_ok);
-                        const bool one = (sup && leq) || (supx && leqx);
-                        if (MIXED && F.ff_one_body) {
-                            // everything in FP32-pair arithmetic, one rounding to double
-                            FF v{0.f, 0.f};
-                            int Ev = 0;
-                            bool has = false;
-                            double wide_re = 0.0;
-                            if (r12 && wide) {
-                                wide_re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2,
-                                                    sup, supx, r_nc, n_d, n_a, n_b, k, W);
+                } else {
+                    for (int e0 = 0; e0 < tot; e0 += 32) {
+                        const int e = e0 + lane;
+                        int pos = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1) {
+                            int cand_pos = pos + step;
+                            int v = __shfl_sync(FULL, excl, cand_pos);
+                            if (v <= e) pos = cand_pos;
+                        }
+                        const int o_ex = __shfl_sync(FULL, excl, pos);
+                        const int r_nc = __shfl_sync(FULL, n_c, pos);
+                        const int r_base = __shfl_sync(FULL, base, pos);
+                        const int r_lo = __shfl_sync(FULL, lo, pos);
+                        const int r_s1 = __shfl_sync(FULL, hs.s1, pos);
+                        const int r_l1 = __shfl_sync(FULL, hs.l1, pos);
+                        const int r_s2 = __shfl_sync(FULL, hs.s2, pos);
+                        if (e < tot) {
+                            const int o = e - o_ex;
+                            const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
+                            const int j = r_base + (n_d - r_lo);
+                            const bool sup = abs(n_a - r_nc) < k && abs(n_b - n_d) < k;
+                            const bool supx = abs(n_a - n_d) < k && abs(n_b - r_nc) < k;
+                            double re = 0.0, im = 0.0;
+                            const bool r12 = (sup && dir_ok) || (supx && ex_ok);
+                            const bool one = (sup && leq) || (supx && leqx);
+                            if (MIXED && F.ff_one_body) {
+                                // everything in FP32-pair arithmetic, one rounding to double
+                                FF v{0.f, 0.f};
+                                int Ev = 0;
+                                bool has = false;
+                                double wide_re = 0.0;
+                                if (r12 && wide) {
+                                    wide_re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2,
+                                                        sup, supx, r_nc, n_d, n_a, n_b, k, W);
+                                } else if (r12) {
+                                    const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
+                                    const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
+                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                    if (sup)
+                                        for (int u = 0; u < pi.nd; ++u)
+                                            ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
+                                    if (supx)
+                                        for (int u = 0; u < pi.nx; ++u)
+                                            ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
+                                    v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                    has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
+                                }
+                                FF hi_im{0.f, 0.f};
+                                if (one) {
+                                    // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
+                                    // term is non-zero only under sup, the l_eq_ex term only
+                                    // under sup_x, so both lookups stay inside the band
+                                    FF hr{0.f, 0.f};
+                                    if (leq && sup) {
+                                        const int dc = r_nc - n_a, dd = n_d - n_b;
+                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                        hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                    ff_mul(make_float2(h2.x, h2.y), s2r));
+                                        hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
+                                    }
+                                    if (leqx && supx) {
+                                        const int dc = n_d - n_a, dd = r_nc - n_b;
+                                        float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                                        float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                                        const bool ng = sgn_bit != 0;
+                                        FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
+                                                       ff_mul(make_float2(h2.x, h2.y), s2r));
+                                        FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
+                                                       ff_mul(make_float2(h2.z, h2.w), s2r));
+                                        hr = ff_add(hr, ff_neg_if(xr, ng));
+                                        hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
+                                    }
+                                    // the one-body part is in absolute scale (exponent
+                                    // kRkBias in the pair's frame), the two-electron part
+                                    // in its slice's frame Ev: joined as FP32 pairs while
+                                    // the factor 2^(Ev - kRkBias) that rescales the latter
+                                    // is a normal float with margin (slice maxima above
+                                    // 2^-12, radii below ~4000 a.u., for kRkBias = 112),
+                                    // in FP64 otherwise
+                                    if (!has || kRkBias - Ev <= 124) {
+                                        v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
+                                        has = true;
+                                    } else {
+                                        re = ff_to_double(hr, 0);
+                                    }
+                                }
+                                if (has) re = re + ff_to_double(v, Ev - kRkBias);
+                                re = re + wide_re;
+                                im = one ? ff_to_double(hi_im, 0) : 0.0;
                             } else if (r12) {
                                 const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
                                 const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
-                                FF fd{0.f, 0.f}, fx{0.f, 0.f};
-                                if (sup)
-                                    for (int u = 0; u < pi.nd; ++u)
-                                        ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
-                                if (supx)
-                                    for (int u = 0; u < pi.nx; ++u)
-                                        ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
-                                v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
-                                has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
+                                if (MIXED && wide) {
+                                    re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2, sup,
+                                                   supx, r_nc, n_d, n_a, n_b, k, W);
+                                } else if (MIXED) {
+                                    FF fd{0.f, 0.f}, fx{0.f, 0.f};
+                                    if (sup)
+                                        for (int u = 0; u < pi.nd; ++u)
+                                            ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
+                                    if (supx)
+                                        for (int u = 0; u < pi.nx; ++u)
+                                            ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
+                                    int Ev;
+                                    FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
+                                    re = ff_to_double(v, Ev - kRkBias);
+                                } else {
+                                    // direct and exchange multipole sums in one accumulator
+                                    // (no FP64 add joins them)
+                                    if (sup) {
+                                        const double *Rt = sR + od;
+                                        for (int u = 0; u < pi.nd; ++u) re = fma(Rt[sKow[0][u]], sAd[0][u], re);
+                                    }
+                                    if (supx) {
+                                        const double *Rt = sR + ox;
+                                        for (int u = 0; u < pi.nx; ++u) re = fma(Rt[sKow[1][u]], sAd[1][u], re);
+                                    }
+                                }
                             }
-                            FF hi_im{0.f, 0.f};
-                            if (one) {
-                                // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
+                            if (one && !(MIXED && F.ff_one_body) && F.s_real) {
+                                // H_1p_neq (mat_els.f90:697-715) with a real S: the l_eq
                                 // term is non-zero only under sup, the l_eq_ex term only
-                                // under sup_x, so both lookups stay inside the band
-                                FF hr{0.f, 0.f};
+                                // under sup_x (both lookups inside the band); its
+                                // products go straight into the entry's accumulators
+                                // and the exchange sign flips the S factors
                                 if (leq && sup) {
                                     const int dc = r_nc - n_a, dd = n_d - n_b;
-                                    float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
-                                    float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
-                                    hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
-                                                ff_mul(make_float2(h2.x, h2.y), s2r));
-                                    hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
-                                                   ff_mul(make_float2(h2.z, h2.w), s2r));
+                                    const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                    const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+                                    re = fma(h1.x, s1, re);
+                                    re = fma(h2.x, s2, re);
+                                    im = fma(h1.y, s1, im);
+                                    im = fma(h2.y, s2, im);
                                 }
                                 if (leqx && supx) {
                                     const int dc = n_d - n_a, dd = r_nc - n_b;
-                                    float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
-                                    float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
-                                    const bool ng = sgn_bit != 0;
-                                    FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r),
-                                                   ff_mul(make_float2(h2.x, h2.y), s2r));
-                                    FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r),
-                                                   ff_mul(make_float2(h2.z, h2.w), s2r));
-                                    hr = ff_add(hr, ff_neg_if(xr, ng));
-                                    hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
+                                    const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                    const double s1 = flip_sign(SbR[dd].x, sgn_bit);
+                                    const double s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                    re = fma(h1.x, s1, re);
+                                    re = fma(h2.x, s2, re);
+                                    im = fma(h1.y, s1, im);
+                                    im = fma(h2.y, s2, im);
                                 }
-                                // the one-body part is in absolute scale (exponent
-                                // kRkBias in the pair's frame), the two-electron part
-                                // in its slice's frame Ev: joined as FP32 pairs while
-                                // the factor 2^(Ev - kRkBias) that rescales the latter
-                                // is a normal float with margin (slice maxima above
-                                // 2^-12, radii below ~4000 a.u., for kRkBias = 112),
-                                // in FP64 otherwise
-                                if (!has || kRkBias - Ev <= 124) {
-                                    v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
-                                    has = true;
-                                } else {
-                                    re = ff_to_double(hr, 0);
+                            } else if (one && !(MIXED && F.ff_one_body)) {
+                                // H_1p_neq (mat_els.f90:697-715), complex S
+                                const int N = A.N;
+                                const double2 *Ha = F.Hb + (size_t)l_a * N * W;
+                                const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
+                                double2 h1 = make_double2(0.0, 0.0);
+                                if (leq) {
+                                    double2 t1 = cmul(band(Ha, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d));
+                                    double2 t2 = cmul(band(Hbb, N, k, n_b, n_d), band(F.Sb, N, k, n_a, r_nc));
+                                    h1 = cadd(cadd(h1, t1), t2);
                                 }
+                                if (leqx) {
+                                    double2 t1 = cmul(band(Ha, N, k, n_a, n_d), band(F.Sb, N, k, n_b, r_nc));
+                                    double2 t2 = cmul(band(Hbb, N, k, n_b, r_nc), band(F.Sb, N, k, n_a, n_d));
+                                    double2 t12 = cadd(t1, t2);
+                                    h1 = cadd(h1, make_double2(t12.x * pi.sgn, t12.y * pi.sgn));
+                                }
+                                re = re + h1.x;
+                                im = im + h1.y;
                             }
-                            if (has) re = re + ff_to_double(v, Ev - kRkBias);
-                            re = re + wide_re;
-                            im = one ? ff_to_double(hi_im, 0) : 0.0;
-                        } else if (r12) {
-                            const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
-                            const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
-                            if (MIXED && wide) {
-                                re = wide_sums(sR2, sexp, kd, kx, ad, ax, pi.nd, pi.nx, W2, sup,
-                                               supx, r_nc, n_d, n_a, n_b, k, W);
-                            } else if (MIXED) {
-                                FF fd{0.f, 0.f}, fx{0.f, 0.f};
-                                if (sup)
-                                    for (int u = 0; u < pi.nd; ++u)
-                                        ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
-                                if (supx)
-                                    for (int u = 0; u < pi.nx; ++u)
-                                        ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
-                                int Ev;
-                                FF v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
-                                re = ff_to_double(v, Ev - kRkBias);
-                            } else {
-                                // direct and exchange multipole sums in one accumulator
-                                // (no FP64 add joins them)
-                                if (sup) {
-                                    const double *Rt = sR + od;
-                                    for (int u = 0; u < pi.nd; ++u) re = fma(Rt[sKow[0][u]], sAd[0][u], re);
-                                }
-                                if (supx) {
-                                    const double *Rt = sR + ox;
-                                    for (int u = 0; u < pi.nx; ++u) re = fma(Rt[sKow[1][u]], sAd[1][u], re);
-                                }
-                            }
+                            F.Hidx[oH + e] = (int64_t)j + 1;
+                            F.Hdat[oH + e] = make_double2(re, im);
                         }
-                        if (one && !(MIXED && F.ff_one_body) && F.s_real) {
-                            // H_1p_neq (mat_els.f90:697-715) with a real S: the l_eq
-                            // term is non-zero only under sup, the l_eq_ex term only
-                            // under sup_x (both lookups inside the band); its
-                            // products go straight into the entry's accumulators
-                            // and the exchange sign flips the S factors
-                            if (leq && sup) {
-                                const int dc = r_nc - n_a, dd = n_d - n_b;
-                                const double2 h1 = HaR[dc], h2 = HbR[dd];
-                                const double s1 = SbR[dd].x, s2 = SaR[dc].x;
-                                re = fma(h1.x, s1, re);
-                                re = fma(h2.x, s2, re);
-                                im = fma(h1.y, s1, im);
-                                im = fma(h2.y, s2, im);
-                            }
-                            if (leqx && supx) {
-                                const int dc = n_d - n_a, dd = r_nc - n_b;
-                                const double2 h1 = HaR[dc], h2 = HbR[dd];
-                                const double s1 = flip_sign(SbR[dd].x, sgn_bit);
-                                const double s2 = flip_sign(SaR[dc].x, sgn_bit);
-                                re = fma(h1.x, s1, re);
-                                re = fma(h2.x, s2, re);
-                                im = fma(h1.y, s1, im);
-                                im = fma(h2.y, s2, im);
-                            }
-                        } else if (one && !(MIXED && F.ff_one_body)) {
-                            // H_1p_neq (mat_els.f90:697-715), complex S
-                            const int N = A.N;
-                            const double2 *Ha = F.Hb + (size_t)l_a * N * W;
-                            const double2 *Hbb = F.Hb + (size_t)l_b * N * W;
-                            double2 h1 = make_double2(0.0, 0.0);
-                            if (leq) {
-                                double2 t1 = cmul(band(Ha, N, k, n_a, r_nc), band(F.Sb, N, k, n_b, n_d));
-                                double2 t2 = cmul(band(Hbb, N, k, n_b, n_d), band(F.Sb, N, k, n_a, r_nc));
-                                h1 = cadd(cadd(h1, t1), t2);
-                            }
-                            if (leqx) {
-                                double2 t1 = cmul(band(Ha, N, k, n_a, n_d), band(F.Sb, N, k, n_b, r_nc));
-                                double2 t2 = cmul(band(Hbb, N, k, n_b, r_nc), band(F.Sb, N, k, n_a, n_d));
-                                double2 t12 = cadd(t1, t2);
-                                h1 = cadd(h1, make_double2(t12.x * pi.sgn, t12.y * pi.sgn));
-                            }
-                            re = re + h1.x;
-                            im = im + h1.y;
-                        }
-                        F.Hidx[oH + e] = (int64_t)j + 1;
-                        F.Hdat[oH + e] = make_double2(re, im);
                     }
                 }
                 oH += tot;

@@ -92,6 +92,28 @@ def test_blocks_match_oracle(bs2e, oracle, case, full):
             assert_csr_close(Sg, Sr, RTOL, with_scale=False)
 
 
+@pytest.mark.parametrize("case", ["small2", "cut"])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_blocks_with_complex_overlap_match_oracle(bs2e, oracle, case, prec):
+    """A complex overlap matrix (as a complex-scaled radial grid gives) takes the
+    fill's complex-S branches of S_mat_neq and H_1p_neq (mat_els.f90:664-715)."""
+    c = CASES[case]
+    ref = oracle_reference(case)
+    S = ref["S"] * (1.0 + 0.3j)
+    precision = bs2e.PREC_FP64 if prec == "fp64" else bs2e.PREC_MIXED
+    tol = RTOL if prec == "fp64" else 1e-11
+    with _handle(bs2e, case, precision=precision) as h:
+        h.rk()
+        h.set_one_body(ref["H1p"], S)
+        for (L, M, par, spin, cf) in blocks(bs2e, case):
+            for full in (True, False):
+                Hg, Sg = h.block(cf, L, full, spin)
+                Hr, Sr = oracle.construct_block(cf, L, c["k"], c["n_b"], c["max_k"], ref["R"],
+                                                ref["H1p"], S, full, spin)
+                assert_csr_close(Hg, Hr, tol)
+                assert_csr_close(Sg, Sr, tol, with_scale=False)
+
+
 def test_device_outputs_match_host_outputs(bs2e, oracle):
     import torch
     c = CASES["small2"]
