@@ -690,37 +690,45 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                             reA = supxA ? a : reA;
                             reB = supxB ? b : reB;
                         }
-                        if (leq && (supA || supB)) {
-                            const int dcA = supA ? ncA - n_a : 0, ddA = supA ? ndA - n_b : 0;
-                            const int dcB = supB ? ncB - n_a : 0, ddB = supB ? ndB - n_b : 0;
-                            const double2 h1A = HaR[dcA], h2A = HbR[ddA], h1B = HaR[dcB], h2B = HbR[ddB];
-                            const double s1A = supA ? SbR[ddA].x : 0.0, s2A = supA ? SaR[dcA].x : 0.0;
-                            const double s1B = supB ? SbR[ddB].x : 0.0, s2B = supB ? SaR[dcB].x : 0.0;
-                            reA = fma(h1A.x, s1A, reA);
-                            reB = fma(h1B.x, s1B, reB);
-                            reA = fma(h2A.x, s2A, reA);
-                            reB = fma(h2B.x, s2B, reB);
-                            imA = fma(h1A.y, s1A, imA);
-                            imB = fma(h1B.y, s1B, imB);
-                            imA = fma(h2A.y, s2A, imA);
-                            imB = fma(h2B.y, s2B, imB);
+                        if (leq) {
+                            if (supA) {
+                                const int dc = ncA - n_a, dd = ndA - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+                                reA = fma(h1.x, s1, reA);
+                                reA = fma(h2.x, s2, reA);
+                                imA = fma(h1.y, s1, imA);
+                                imA = fma(h2.y, s2, imA);
+                            }
+                            if (supB) {
+                                const int dc = ncB - n_a, dd = ndB - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+                                reB = fma(h1.x, s1, reB);
+                                reB = fma(h2.x, s2, reB);
+                                imB = fma(h1.y, s1, imB);
+                                imB = fma(h2.y, s2, imB);
+                            }
                         }
-                        if (leqx && (supxA || supxB)) {
-                            const int dcA = supxA ? ndA - n_a : 0, ddA = supxA ? ncA - n_b : 0;
-                            const int dcB = supxB ? ndB - n_a : 0, ddB = supxB ? ncB - n_b : 0;
-                            const double2 h1A = HaR[dcA], h2A = HbR[ddA], h1B = HaR[dcB], h2B = HbR[ddB];
-                            const double s1A = supxA ? flip_sign(SbR[ddA].x, sgn_bit) : 0.0;
-                            const double s2A = supxA ? flip_sign(SaR[dcA].x, sgn_bit) : 0.0;
-                            const double s1B = supxB ? flip_sign(SbR[ddB].x, sgn_bit) : 0.0;
-                            const double s2B = supxB ? flip_sign(SaR[dcB].x, sgn_bit) : 0.0;
-                            reA = fma(h1A.x, s1A, reA);
-                            reB = fma(h1B.x, s1B, reB);
-                            reA = fma(h2A.x, s2A, reA);
-                            reB = fma(h2B.x, s2B, reB);
-                            imA = fma(h1A.y, s1A, imA);
-                            imB = fma(h1B.y, s1B, imB);
-                            imA = fma(h2A.y, s2A, imA);
-                            imB = fma(h2B.y, s2B, imB);
+                        if (leqx) {
+                            if (supxA) {
+                                const int dc = ndA - n_a, dd = ncA - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = flip_sign(SbR[dd].x, sgn_bit), s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                reA = fma(h1.x, s1, reA);
+                                reA = fma(h2.x, s2, reA);
+                                imA = fma(h1.y, s1, imA);
+                                imA = fma(h2.y, s2, imA);
+                            }
+                            if (supxB) {
+                                const int dc = ndB - n_a, dd = ncB - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = flip_sign(SbR[dd].x, sgn_bit), s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                reB = fma(h1.x, s1, reB);
+                                reB = fma(h2.x, s2, reB);
+                                imB = fma(h1.y, s1, imB);
+                                imB = fma(h2.y, s2, imB);
+                            }
                         }
                         if (liveA) {
                             F.Hidx[oH + eA] = (int64_t)jA + 1;
