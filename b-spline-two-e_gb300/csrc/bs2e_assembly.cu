@@ -788,6 +788,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                     has = (sup && pi.nd > 0) || (supx && pi.nx > 0);
                                 }
                                 FF hi_im{0.f, 0.f};
+                                bool fb = false;
                                 if (one) {
                                     // H_1p_neq (mat_els.f90:697-715) with real S: the l_eq
                                     // term is non-zero only under sup, the l_eq_ex term only
@@ -825,11 +826,16 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                         v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
                                         has = true;
                                     } else {
+                                        fb = true;
                                         re = ff_to_double(hr, 0);
                                     }
                                 }
-                                if (has) re = re + ff_to_double(v, Ev - kRkBias);
-                                re = re + wide_re;
+                                if (has) {
+                                    const double t = ff_to_double(v, Ev - kRkBias);
+                                    if (fb) re = re + t;
+                                    else re = t;
+                                }
+                                if (wide) re = re + wide_re;
                                 im = one ? ff_to_double(hi_im, 0) : 0.0;
                             } else if (r12) {
                                 const int od = (r_nc - n_a + k - 1) * W + (n_d - n_b + k - 1);
