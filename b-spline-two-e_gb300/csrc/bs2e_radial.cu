@@ -8,6 +8,8 @@
 // (one-body S and H).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "bs2e_internal.h"
 
 namespace bs2e {
@@ -69,9 +71,10 @@ __device__ __forceinline__ double powi(double x, int n) {
 }
 
 // ---------------------------------------------------------------------------
-// K1: tabulation.  One CTA per breakpoint interval.
+// K1: tabulation.  Part `part` of `nparts` CTAs of a breakpoint interval (the
+// batched stage runs a whole interval per work item: part 0 of 1).
 // ---------------------------------------------------------------------------
-__device__ void tabulate_iv(const RadialDev &P, int iv) {
+__device__ void tabulate_iv(const RadialDev &P, int iv, int part = 0, int nparts = 1) {
     const int k = P.k, q = P.q;
     const double *__restrict__ knots = P.knots;
     const double *__restrict__ glx = P.glx;
@@ -79,7 +82,8 @@ __device__ void tabulate_iv(const RadialDev &P, int iv) {
     const double lo = knots[k - 1 + iv], hi = knots[k + iv];
     const double sc = __dmul_rn(0.5, __dsub_rn(hi, lo));
     const double tr = __dmul_rn(0.5, __dadd_rn(hi, lo));
-    for (int e = threadIdx.x; e < q * k; e += blockDim.x) {
+    const int e0 = part * blockDim.x + threadIdx.x, es = nparts * blockDim.x;
+    for (int e = e0; e < q * k; e += es) {
         int Pp = e / k, s = e - Pp * k;
         double r = __dadd_rn(__dmul_rn(sc, glx[Pp]), tr);
         if (s == 0) P.tab_r[(size_t)iv * q + Pp] = r;
@@ -87,7 +91,7 @@ __device__ void tabulate_iv(const RadialDev &P, int iv) {
         P.tab_D2[((size_t)iv * q + Pp) * k + s] = bval(knots, k, r, 2, iv1, iv1 + s);
         P.tab_D1[((size_t)iv * q + Pp) * k + s] = bval(knots, k, r, 1, iv1, iv1 + s);
     }
-    for (int e = threadIdx.x; e < q * q * k; e += blockDim.x) {
+    for (int e = e0; e < q * q * k; e += es) {
         int s = e % k, PQ = e / k, Q = PQ % q, Pp = PQ / q;
         double r = __dadd_rn(__dmul_rn(sc, glx[Pp]), tr);
         double scj = __dmul_rn(0.5, __dsub_rn(r, lo));
@@ -99,7 +103,7 @@ __device__ void tabulate_iv(const RadialDev &P, int iv) {
     }
 }
 
-__global__ void k_tabulate(RadialDev P) { tabulate_iv(P, blockIdx.x); }
+__global__ void k_tabulate(RadialDev P) { tabulate_iv(P, blockIdx.x, blockIdx.y, gridDim.y); }
 
 // ---------------------------------------------------------------------------
 // K2: moments and same-interval integrals.  One CTA per (interval, multipole).
@@ -571,24 +575,30 @@ __global__ void k_one_body(const double *__restrict__ knots, const double *__res
                            const double *__restrict__ tab_D2, int k, int q, int N, int n_iv,
                            int Z, int n_l, int cap_order, double cap_r0, double eta_re,
                            double eta_im, double2 *__restrict__ Sb, double2 *__restrict__ Hb) {
+    // one warp per band entry: the lanes take the (interval, point) terms of
+    // its quadrature and a shuffle reduction sums them
     const int W = 2 * k - 1;
-    int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (e >= (int64_t)n_l * N * W) return;
+    const int64_t e = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (e >= (int64_t)n_l * N * W) return;  // whole warp
     const int l = (int)(e / ((int64_t)N * W));
     const int r = (int)(e - (int64_t)l * N * W);
     const int i = r / W, dx = r - i * W;  // 0-based basis index i, column j = i + dx - (k-1)
     const int j = i + dx - (k - 1);
     if (j < 0 || j >= N) {
-        Hb[e] = make_double2(0.0, 0.0);
-        if (l == 0) Sb[r] = make_double2(0.0, 0.0);
+        if (lane == 0) {
+            Hb[e] = make_double2(0.0, 0.0);
+            if (l == 0) Sb[r] = make_double2(0.0, 0.0);
+        }
         return;
     }
     double s = 0.0, hre = 0.0, him = 0.0;
     const int lo = max(max(i, j) - k + 2, 0), hi = min(min(i, j) + 1, n_iv - 1);
-    for (int iv = lo; iv <= hi; ++iv) {
+    for (int t = lane; t < (hi - lo + 1) * q; t += 32) {
+        const int iv = lo + t / q, P = t - (iv - lo) * q;
         const double a = knots[k - 1 + iv], b = knots[k + iv];
         const int si = i + 1 - iv, sj = j + 1 - iv;
-        for (int P = 0; P < q; ++P) {
+        {
             const size_t o = ((size_t)iv * q + P) * k;
             const double x = tab_r[(size_t)iv * q + P];
             const double w = 0.5 * (b - a) * glw[P];
@@ -605,8 +615,15 @@ __global__ void k_one_body(const double *__restrict__ knots, const double *__res
             him = him + w * (cim * Bi * Bj);
         }
     }
-    Hb[e] = make_double2(hre, him);
-    if (l == 0) Sb[r] = make_double2(s, 0.0);
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        hre += __shfl_xor_sync(0xffffffffu, hre, o);
+        him += __shfl_xor_sync(0xffffffffu, him, o);
+    }
+    if (lane == 0) {
+        Hb[e] = make_double2(hre, him);
+        if (l == 0) Sb[r] = make_double2(s, 0.0);
+    }
 }
 
 // Splits the complex FP64 bands into FP32 pairs (re hi, re lo, im hi, im lo)
@@ -680,7 +697,10 @@ RadialDev radial_dev(const bs2e_handle *h) {
 
 void launch_tabulate(bs2e_handle *h) {
     const Radial &g = h->g;
-    k_tabulate<<<g.n_iv, 128, 0, h->stream>>>(radial_dev(h));
+    // several CTAs per interval: each de Boor evaluation is a long serial chain
+    // of FP64 divisions, so the launch needs many resident warps
+    const int parts = std::max(1, std::min(8, (g.q * g.q * g.k + 127) / 128));
+    k_tabulate<<<dim3((unsigned)g.n_iv, (unsigned)parts), 128, 0, h->stream>>>(radial_dev(h));
     h->launches++;
 }
 
@@ -795,7 +815,7 @@ void launch_one_body(bs2e_handle *h, int64_t Z, int64_t n_l, int64_t cap_order, 
                      double eta_re, double eta_im) {
     const Radial &g = h->g;
     int64_t n = n_l * g.N * g.W;
-    k_one_body<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(
+    k_one_body<<<(unsigned)((n * 32 + 127) / 128), 128, 0, h->stream>>>(
         h->d_knots, h->d_glw, h->d_tab_r, h->d_tab_B, h->d_tab_D2, g.k, g.q, g.N, g.n_iv, (int)Z,
         (int)n_l, (int)cap_order, cap_r0, eta_re, eta_im, h->d_Sb, h->d_Hb);
     h->launches++;
