@@ -239,38 +239,6 @@ __global__ void k_totals(RadialDev P) {
 // precision (2^108 at the N=200, k=0..10 grid; about 2^200 at k=20 on the
 // N=800, r_max=800 grid).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double rk_element(const double *__restrict__ mom,
-                                            const double *__restrict__ dint,
-                                            const double *__restrict__ tot, int k, int K1, int N,
-                                            int n_iv, int a, int b, int kk, int dc, int dd) {
-    const int W = 2 * k - 1, k2 = k * k;
-    int c = a + dc - (k - 1), d = b + dd - (k - 1);
-    if (c < 0 || c >= N || d < 0 || d >= N) return 0.0;
-    int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-    int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
-    const double *mt = tot + (size_t)kk * N * W;
-    const double *Mt = tot + ((size_t)K1 + kk) * N * W;
-    if (hip < loq) return mt[a * W + dc] * Mt[b * W + dd];
-    if (lop > hiq) return Mt[a * W + dc] * mt[b * W + dd];
-    double v = 0.0;
-    for (int iv1 = lop; iv1 <= hip; ++iv1) {
-        int pa = (a + 1 - iv1) * k + (c + 1 - iv1);
-        const double *m1 = mom + ((size_t)iv1 * K1 + kk) * 2 * k2;
-        for (int iv2 = loq; iv2 <= hiq; ++iv2) {
-            int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
-            const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
-            if (iv1 < iv2) {
-                v = fma(m1[pa], m2[k2 + pb], v);
-            } else if (iv1 > iv2) {
-                v = fma(m1[k2 + pa], m2[pb], v);
-            } else {
-                const double *D = dint + ((size_t)iv1 * K1 + kk) * (size_t)k2 * k2;
-                v += D[(size_t)pa * k2 + pb] + D[(size_t)pb * k2 + pa];
-            }
-        }
-    }
-    return v;
-}
 
 // Near-field tiles (|a - b| < k, where the interval ranges of an (a, c) pair
 // and a (b, d) pair can meet).  With iv2_j = b - k + 2 + j (j < k) the
@@ -345,16 +313,41 @@ __host__ __device__ __forceinline__ size_t rk_near_scratch(int k) {
 }
 
 // Values of multipoles [k_first, k_first + k_count) of tile t = a * N + b:
-// out[kk * W^2 + dc * W + dd] (block-wide; s: rk_near_scratch doubles).
+// out[kk * W^2 + dc * W + dd] (block-wide; s: rk_near_scratch doubles).  Each
+// thread keeps its window positions r = dc * W + dd (r = threadIdx.x + i *
+// blockDim.x) and walks them with an incremental (dc, dd), so no element pays
+// an integer division.
 __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k_count,
                                double *out, double *s) {
     const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
     const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
-    if (abs(a - b) >= k) {  // far field everywhere: products of pair totals
-        for (int e = threadIdx.x; e < k_count * W2; e += blockDim.x) {
-            const int kk = k_first + e / W2, r = e % W2;
-            out[kk * W2 + r] = rk_element(P.mom, P.dint, P.tot, k, K1, N, P.n_iv, a, b, kk,
-                                          r / W, r % W);
+    const int step_dc = blockDim.x / W, step_dd = blockDim.x - step_dc * W;
+    const int dc0 = threadIdx.x / W, dd0 = threadIdx.x - dc0 * W;
+    if (abs(a - b) >= k) {
+        // far field everywhere: the (a, c) intervals lie all below the (b, d)
+        // ones when a < b, all above when a > b, so R^k is the product of the
+        // pair totals, m_k(ac) M_k(bd) or M_k(ac) m_k(bd)
+        // (sparse_array_tools.f90:452-493 sums the same interval products)
+        const size_t NW = (size_t)N * W, lower = a < b ? 0 : (size_t)K1 * NW;
+        const size_t upper = a < b ? (size_t)K1 * NW : 0;
+        int dc = dc0, dd = dd0;
+        for (int r = threadIdx.x; r < W2; r += blockDim.x) {
+            const int c = a + dc - (k - 1), d = b + dd - (k - 1);
+            double *o = out + r;
+            if (c < 0 || c >= N || d < 0 || d >= N) {
+                for (int kk = k_first; kk < k_first + k_count; ++kk) o[kk * W2] = 0.0;
+            } else {
+                const double *x1 = P.tot + lower + (size_t)a * W + dc;
+                const double *x2 = P.tot + upper + (size_t)b * W + dd;
+                for (int kk = k_first; kk < k_first + k_count; ++kk)
+                    o[kk * W2] = x1[kk * NW] * x2[kk * NW];
+            }
+            dc += step_dc;
+            dd += step_dd;
+            if (dd >= W) {
+                dd -= W;
+                ++dc;
+            }
         }
         return;
     }
@@ -362,8 +355,16 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
         __syncthreads();
         rk_near_stage(P, a, b, kk, s);
         __syncthreads();
-        for (int r = threadIdx.x; r < W2; r += blockDim.x)
-            out[kk * W2 + r] = rk_near_element(P, s, a, b, kk, r / W, r % W);
+        int dc = dc0, dd = dd0;
+        for (int r = threadIdx.x; r < W2; r += blockDim.x) {
+            out[kk * W2 + r] = rk_near_element(P, s, a, b, kk, dc, dd);
+            dc += step_dc;
+            dd += step_dd;
+            if (dd >= W) {
+                dd -= W;
+                ++dc;
+            }
+        }
     }
 }
 
@@ -396,18 +397,16 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
     }
     __syncthreads();
     float2 *dst = P.Rf + (size_t)t * P.tile;
-    for (int e = threadIdx.x; e < P.tile; e += blockDim.x) {
-        if (e >= nel) {
-            dst[e] = make_float2(0.f, 0.f);
-            continue;
+    for (int e = nel + threadIdx.x; e < P.tile; e += blockDim.x) dst[e] = make_float2(0.f, 0.f);
+    for (int kk = k_first; kk < k_first + k_count; ++kk) {
+        const double scale = __longlong_as_double((long long)(1023 + kRkBias - sexp[kk]) << 52);
+        for (int r = threadIdx.x; r < W2; r += blockDim.x) {
+            const int e = kk * W2 + r;
+            double x = sv[e] * scale;
+            float hi = __double2float_rn(x);
+            float lo = __double2float_rn(x - (double)hi);
+            dst[e] = make_float2(hi, lo);
         }
-        int kk = e / W2;
-        if (kk < k_first || kk >= k_first + k_count) continue;
-        double scale = __longlong_as_double((long long)(1023 + kRkBias - sexp[kk]) << 52);
-        double x = sv[e] * scale;
-        float hi = __double2float_rn(x);
-        float lo = __double2float_rn(x - (double)hi);
-        dst[e] = make_float2(hi, lo);
     }
 }
 
