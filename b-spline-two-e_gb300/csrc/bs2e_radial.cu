@@ -174,13 +174,21 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
     }
     __syncthreads();
     const size_t dbase = ((size_t)iv * K1 + kk) * (size_t)k2 * k2;
+    // (p, qq) of e = p * k2 + qq walked incrementally (no division per element)
+    const int step_p = blockDim.x / k2, step_q = blockDim.x - step_p * k2;
+    int p = threadIdx.x / k2, qq = threadIdx.x - p * k2;
     for (int e = threadIdx.x; e < k2 * k2; e += blockDim.x) {
-        int p = e / k2, qq = e - p * k2;
         const double *o = sO + p * q;
         const double *jj = sJ + qq * q;
         double acc = 0.0;
         for (int P = 0; P < q; ++P) acc = fma(o[P], jj[P], acc);
         dint[dbase + e] = h * acc;
+        p += step_p;
+        qq += step_q;
+        if (qq >= k2) {
+            qq -= k2;
+            ++p;
+        }
     }
 }
 
