@@ -668,6 +668,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                             const int oA = supA ? (ncA - n_a + k - 1) * W + (ndA - n_b + k - 1) : 0;
                             const int oB = supB ? (ncB - n_a + k - 1) * W + (ndB - n_b + k - 1) : 0;
                             double a = 0.0, b = 0.0;
+#pragma unroll 4
                             for (int u = 0; u < pi.nd; ++u) {
                                 const int ko = sKow[0][u];
                                 const double w = sAd[0][u];
@@ -681,6 +682,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                             const int oA = supxA ? (ndA - n_a + k - 1) * W + (ncA - n_b + k - 1) : 0;
                             const int oB = supxB ? (ndB - n_a + k - 1) * W + (ncB - n_b + k - 1) : 0;
                             double a = reA, b = reB;
+#pragma unroll 4
                             for (int u = 0; u < pi.nx; ++u) {
                                 const int ko = sKow[1][u];
                                 const double w = sAd[1][u];
@@ -779,9 +781,11 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                     const int ox = (n_d - n_a + k - 1) * W + (r_nc - n_b + k - 1);
                                     FF fd{0.f, 0.f}, fx{0.f, 0.f};
                                     if (sup)
+#pragma unroll 4
                                         for (int u = 0; u < pi.nd; ++u)
                                             ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
                                     if (supx)
+#pragma unroll 4
                                         for (int u = 0; u < pi.nx; ++u)
                                             ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
                                     v = ff_join(fd, Ed, sup && pi.nd > 0, fx, Ex, supx && pi.nx > 0, Ev);
@@ -846,9 +850,11 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                                 } else if (MIXED) {
                                     FF fd{0.f, 0.f}, fx{0.f, 0.f};
                                     if (sup)
+#pragma unroll 4
                                         for (int u = 0; u < pi.nd; ++u)
                                             ff_madd(fd, sAw[0][u], sR2[sKow[0][u] + od]);
                                     if (supx)
+#pragma unroll 4
                                         for (int u = 0; u < pi.nx; ++u)
                                             ff_madd(fx, sAw[1][u], sR2[sKow[1][u] + ox]);
                                     int Ev;
