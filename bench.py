@@ -58,7 +58,7 @@ WORKLOAD = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5, max_L=3, Z=2
 # dram__bytes_read.sum + dram__bytes_write.sum of the k_csr_fill launch on
 # block 0 (ncu --set full, profiles/k_csr_fill_order7_n200_block0.md) and that
 # launch's algorithmic bytes (3,154,438,224 B of CSR + 20,100 staged tiles).
-NCU_BLOCK0_DRAM = {"fp64": 3484750848.0, "mixed": 3669510912.0}
+NCU_BLOCK0_DRAM = {"fp64": 3478840576.0, "mixed": 3683740672.0}
 NCU_BLOCK0_ALG = 3453526224.0
 
 
