@@ -475,10 +475,10 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
 // Minimum resident CTAs per SM the fill kernel is compiled for (caps its
 // registers at 65536 / (128 * this)), for the mixed and the FP64 kernel.
 // Measured on the order-7, N=200, k=0..10, l_max=5, L=0..3 singlet+triplet
-// workload (fill time per step): mixed 8 -> 42.7 ms (64 registers), 6 ->
-// 45.9, 4 -> 50.7; FP64 8 -> 28.3 ms, 6 -> 32.1 (80 registers), 10 -> 35.8
-// (48, spilling), 12 -> 40.5.  Fewer registers spill in the entry loop, more
-// leave too few warps to hide the FP64 and shuffle latencies.
+// workload (fill time per step): mixed 8 -> 46.8 ms (64 registers), 7 ->
+// 48.9 (72), 6 -> 49.4 (80); FP64 8 -> 28.3 ms, 6 -> 32.1 (80 registers), 10
+// -> 35.8 (48, spilling), 12 -> 40.5.  Fewer registers spill in the entry
+// loop, more leave too few warps to hide the FP64 and shuffle latencies.
 #ifndef BS2E_FILL_MIN_BLOCKS
 #define BS2E_FILL_MIN_BLOCKS 8
 #endif
