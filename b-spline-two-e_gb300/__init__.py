@@ -38,7 +38,8 @@ EXPORTS = [
     "bs2e_default_opts", "bs2e_create", "bs2e_destroy", "bs2e_last_error", "bs2e_sizes",
     "bs2e_slater", "bs2e_get_primitives", "bs2e_rk", "bs2e_rk_get", "bs2e_rk_get_batch",
     "bs2e_set_one_body", "bs2e_one_body", "bs2e_block_count", "bs2e_block_fill",
-    "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_configs", "bs2e_ang_k_LS",
+    "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_blocks_count_all",
+    "bs2e_blocks_fill_all", "bs2e_configs", "bs2e_ang_k_LS",
     "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
     "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
     "bs2e_rk_get_batch_static", "bs2e_write_block_diag", "bs2e_write_block",
@@ -101,6 +102,8 @@ def lib():
         "bs2e_block_fill": (st, [p, p, i64, i64, i64, p, i64, p, p, p, p, p, p, p]),
         "bs2e_block_count_ex": (st, [p, p, i64, i64, i64, i64, p, p]),
         "bs2e_block_fill_ex": (st, [p, p, i64, i64, i64, i64, p, p, p, p, p, p, i64]),
+        "bs2e_blocks_count_all": (st, [p, i64, p, p, p, p, i64, p, p]),
+        "bs2e_blocks_fill_all": (st, [p, i64, p, p, p, p, i64, p, p, p, p, p, p, i64]),
         "bs2e_configs": (st, [i64, i64, i64, i64, i64, i64, i64, i64, i64, p, p]),
         "bs2e_ang_k_LS": (dbl, [i64, i64, i64, i64, i64, i64]),
         "bs2e_three_j": (dbl, [i64, i64, i64, i64, i64, i64]),
@@ -376,6 +379,53 @@ class Bs2e:
             args += [_ptr(S[x]) for x in ("index_ptr", "indices", "data")]
         _check(self._h, lib().bs2e_block_fill_ex(self._h, _ptr(cf), cf.size, int(L), int(spin),
                                                  int(bool(full)), *args, int(bool(on_device))))
+
+    # -- all symmetry blocks in one call ---------------------------------------
+    @staticmethod
+    def _blocks_args(blocks):
+        cfs = [as_configs(cf) for (cf, L, spin) in blocks]
+        n = len(cfs)
+        ptrs = (ctypes.c_void_p * max(n, 1))(*[cf.ctypes.data for cf in cfs])
+        n_config = np.array([cf.size for cf in cfs], dtype=np.int64)
+        Ls = np.array([int(L) for (_, L, _) in blocks], dtype=np.int64)
+        spins = np.array([int(sp) for (_, _, sp) in blocks], dtype=np.int64)
+        return cfs, ptrs, n_config, Ls, spins
+
+    def blocks_count_all(self, blocks, full=True):
+        """bs2e_blocks_count_all over blocks = [(configs, L, spin), ...];
+        returns (nnz_H, nnz_S) int64 arrays."""
+        cfs, ptrs, n_config, Ls, spins = self._blocks_args(blocks)
+        nH = np.zeros(len(cfs), dtype=np.int64)
+        nS = np.zeros(len(cfs), dtype=np.int64)
+        _check(self._h, lib().bs2e_blocks_count_all(self._h, len(cfs), ptrs, _ptr(n_config),
+                                                    _ptr(Ls), _ptr(spins), int(bool(full)),
+                                                    _ptr(nH), _ptr(nS)))
+        return nH, nS
+
+    def blocks_fill_all_into(self, blocks, full, Hs, Ss, on_device=False):
+        """bs2e_blocks_fill_all into caller arrays: Hs[i], Ss[i] are dicts as in
+        block_fill_into (numpy arrays, or device addresses with on_device)."""
+        cfs, ptrs, n_config, Ls, spins = self._blocks_args(blocks)
+        n = max(len(cfs), 1)
+        addr = (lambda v: int(v)) if on_device else (lambda v: v.ctypes.data)
+        arr = lambda D, x: (ctypes.c_void_p * n)(*[addr(d[x]) for d in D])
+        _check(self._h, lib().bs2e_blocks_fill_all(
+            self._h, len(cfs), ptrs, _ptr(n_config), _ptr(Ls), _ptr(spins), int(bool(full)),
+            arr(Hs, "index_ptr"), arr(Hs, "indices"), arr(Hs, "data"),
+            arr(Ss, "index_ptr"), arr(Ss, "indices"), arr(Ss, "data"), int(bool(on_device))))
+
+    def blocks_all(self, blocks, full=True):
+        """Count and fill every block into host arrays; returns [(H, S), ...]."""
+        nH, nS = self.blocks_count_all(blocks, full)
+        Hs, Ss = [], []
+        for (cf, L, spin), h, s in zip(blocks, nH, nS):
+            n = as_configs(cf).size
+            Hs.append(dict(shape=(n, n), nnz=int(h), index_ptr=np.zeros(n + 1, np.int64),
+                           indices=np.zeros(h, np.int64), data=np.zeros(h, np.complex128)))
+            Ss.append(dict(shape=(n, n), nnz=int(s), index_ptr=np.zeros(n + 1, np.int64),
+                           indices=np.zeros(s, np.int64), data=np.zeros(s, np.complex128)))
+        self.blocks_fill_all_into(blocks, full, Hs, Ss)
+        return list(zip(Hs, Ss))
 
     # -- dipoles ---------------------------------------------------------------
     def radial_dipole(self, gauge=0, copy_out=True):

@@ -1097,6 +1097,61 @@ BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *confi
     return sync_check(h, "block fill");
 }
 
+// All symmetry blocks of a basis in one call: the loop of main_basis_setup.f90
+// :105-116 over bas%syms as a batched count and a batched fill.  Each block
+// goes through the single-block entry points (which take the handle's lock);
+// the counts leave every block in the handle's block cache, so the fills that
+// follow reuse their plans.  A failure names the block it happened in.
+static bs2e_status blocks_args_ok(int64_t n_blocks, const bs2e_config *const *configs,
+                                  const int64_t *n_config, const int64_t *L, const int64_t *spin) {
+    if (n_blocks < 0) return BS2E_ERR_ARG;
+    if (n_blocks > 0 && (!configs || !n_config || !L || !spin)) return BS2E_ERR_ARG;
+    return BS2E_OK;
+}
+
+static bs2e_status block_failed(bs2e_handle *h, int64_t i, bs2e_status st) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->err = "block " + std::to_string(i) + ": " + h->err;
+    return st;
+}
+
+BS2E_API bs2e_status bs2e_blocks_count_all(bs2e_handle *h, int64_t n_blocks,
+                                           const bs2e_config *const *configs,
+                                           const int64_t *n_config, const int64_t *L,
+                                           const int64_t *spin, int64_t full, int64_t *nnz_H,
+                                           int64_t *nnz_S) {
+    if (!h || blocks_args_ok(n_blocks, configs, n_config, L, spin) != BS2E_OK ||
+        (n_blocks > 0 && (!nnz_H || !nnz_S)))
+        return BS2E_ERR_ARG;
+    for (int64_t i = 0; i < n_blocks; ++i) {
+        const bs2e_status st = bs2e_block_count_ex(h, configs[i], n_config[i], L[i], spin[i], full,
+                                                   &nnz_H[i], &nnz_S[i]);
+        if (st != BS2E_OK) return block_failed(h, i, st);
+    }
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_blocks_fill_all(bs2e_handle *h, int64_t n_blocks,
+                                          const bs2e_config *const *configs,
+                                          const int64_t *n_config, const int64_t *L,
+                                          const int64_t *spin, int64_t full,
+                                          int64_t *const *H_index_ptr, int64_t *const *H_indices,
+                                          double *const *H_data, int64_t *const *S_index_ptr,
+                                          int64_t *const *S_indices, double *const *S_data,
+                                          int64_t out_on_device) {
+    if (!h || blocks_args_ok(n_blocks, configs, n_config, L, spin) != BS2E_OK ||
+        (n_blocks > 0 && (!H_index_ptr || !H_indices || !H_data || !S_index_ptr ||
+                          !S_indices || !S_data)))
+        return BS2E_ERR_ARG;
+    for (int64_t i = 0; i < n_blocks; ++i) {
+        const bs2e_status st = bs2e_block_fill_ex(
+            h, configs[i], n_config[i], L[i], spin[i], full, H_index_ptr[i], H_indices[i],
+            H_data[i], S_index_ptr[i], S_indices[i], S_data[i], out_on_device);
+        if (st != BS2E_OK) return block_failed(h, i, st);
+    }
+    return BS2E_OK;
+}
+
 // Rows [row_first, row_first + row_count) of a block.
 static bs2e_status check_rows(bs2e_handle *h, int64_t n_config, int64_t row_first, int64_t row_count) {
     if (row_first < 0 || row_count < 0 || row_first + row_count > n_config)

@@ -99,6 +99,30 @@ module bs2e_gpu
             complex(c_double_complex), intent(out) :: S_data(*)
         end function
 
+        ! every symmetry block in one call: configs, H_*, S_* are arrays of
+        ! c_loc() addresses (one per block), n_config, L, spin, nnz_* per block
+        integer(c_int32_t) function bs2e_blocks_count_all(h, n_blocks, configs, n_config, L, &
+                spin, full, nnz_H, nnz_S) bind(C, name="bs2e_blocks_count_all")
+            import :: c_int32_t, c_int64_t, c_ptr
+            type(c_ptr), value :: h
+            integer(c_int64_t), value :: n_blocks, full
+            type(c_ptr), intent(in) :: configs(*)
+            integer(c_int64_t), intent(in) :: n_config(*), L(*), spin(*)
+            integer(c_int64_t), intent(out) :: nnz_H(*), nnz_S(*)
+        end function
+
+        integer(c_int32_t) function bs2e_blocks_fill_all(h, n_blocks, configs, n_config, L, &
+                spin, full, H_index_ptr, H_indices, H_data, S_index_ptr, S_indices, S_data, &
+                out_on_device) bind(C, name="bs2e_blocks_fill_all")
+            import :: c_int32_t, c_int64_t, c_ptr
+            type(c_ptr), value :: h
+            integer(c_int64_t), value :: n_blocks, full, out_on_device
+            type(c_ptr), intent(in) :: configs(*)
+            integer(c_int64_t), intent(in) :: n_config(*), L(*), spin(*)
+            type(c_ptr), intent(in) :: H_index_ptr(*), H_indices(*), H_data(*)
+            type(c_ptr), intent(in) :: S_index_ptr(*), S_indices(*), S_data(*)
+        end function
+
         ! rows row_first .. row_first+row_count-1 (0-based first row) of a block,
         ! range-local index_ptr; spin = 0 singlet, 1 triplet
         integer(c_int32_t) function bs2e_block_count_rows(h, configs, n_config, L, spin, full, &

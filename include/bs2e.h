@@ -190,6 +190,31 @@ BS2E_API bs2e_status bs2e_block_fill_ex(bs2e_handle *h, const bs2e_config *confi
                                         int64_t *S_index_ptr, int64_t *S_indices, double *S_data,
                                         int64_t out_on_device);
 
+/* Every symmetry block of a basis in one call: replaces the OpenMP loop of
+ * construct_block_tensor over bas%syms (main_basis_setup.f90:105-116), so a
+ * shim can make one call outside any parallel region.  Block i is
+ * (configs[i], n_config[i], L[i], spin[i]); full applies to all.
+ * count_all writes nnz_H[i], nnz_S[i]; fill_all writes block i into
+ * H_index_ptr[i], H_indices[i], H_data[i], S_index_ptr[i], S_indices[i],
+ * S_data[i] (sized by the counts; host or device arrays as in
+ * bs2e_block_fill_ex).  The blocks run one after another through the
+ * single-block calls; counting first leaves up to 17 blocks (of at most 2^26
+ * rows each) in the handle's block cache for the fills.  On failure the error
+ * message starts with "block i:". */
+BS2E_API bs2e_status bs2e_blocks_count_all(bs2e_handle *h, int64_t n_blocks,
+                                           const bs2e_config *const *configs,
+                                           const int64_t *n_config, const int64_t *L,
+                                           const int64_t *spin, int64_t full, int64_t *nnz_H,
+                                           int64_t *nnz_S);
+BS2E_API bs2e_status bs2e_blocks_fill_all(bs2e_handle *h, int64_t n_blocks,
+                                          const bs2e_config *const *configs,
+                                          const int64_t *n_config, const int64_t *L,
+                                          const int64_t *spin, int64_t full,
+                                          int64_t *const *H_index_ptr, int64_t *const *H_indices,
+                                          double *const *H_data, int64_t *const *S_index_ptr,
+                                          int64_t *const *S_indices, double *const *S_data,
+                                          int64_t out_on_device);
+
 /* Configuration list of one symmetry block, as count_configs
  * (src/tools/orbital_tools.f90:119-216) with consistent() (:46-72); spin as
  * above.  Returns the count in *n_config and writes the list when out != NULL. */

@@ -100,6 +100,16 @@ def test_create_rejects_bad_input_without_gpu(bs2e):
     assert L.bs2e_create(bs2e._ptr(t), t.size, 6, 0, 2, None, ctypes.byref(h)) == 1  # q < 1
 
 
+def test_batched_block_calls_reject_bad_arguments_without_gpu(bs2e):
+    L = bs2e.lib()
+    z = np.zeros(1, dtype=np.int64)
+    p = bs2e._ptr
+    # no handle, and a negative block count: rejected before any device work
+    assert L.bs2e_blocks_count_all(None, 1, None, p(z), p(z), p(z), 1, p(z), p(z)) == 1
+    assert L.bs2e_blocks_fill_all(None, 0, None, None, None, None, 1, None, None, None, None,
+                                  None, None, 0) == 1
+
+
 @pytest.mark.skipif(gpu_available(), reason="checks the no-GPU failure path")
 def test_compute_path_fails_loudly_without_gpu(bs2e):
     t = bs2e.grids.explin_knots(6, 30, 30.0)
