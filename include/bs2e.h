@@ -369,7 +369,12 @@ BS2E_API bs2e_status bs2e_batch_tuning(const bs2e_batch *b, int64_t *rk_threads,
 BS2E_API bs2e_status bs2e_batch_destroy(bs2e_batch *b);
 
 /* The CUDA stream all work of the handle runs on (cudaStream_t as void*), the
- * number of kernels the handle has launched so far, and a full synchronize. */
+ * number of kernels the handle has launched so far, and a full synchronize.
+ * Device-pointer inputs (out_on_device / on_device calls) are read on this
+ * stream without waiting for other streams: work that produces them on
+ * another stream must be complete (or ordered before this stream with an
+ * event) when the call is made.  Every entry point has finished its device
+ * work on this stream when it returns. */
 BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream);
 BS2E_API bs2e_status bs2e_launch_count(const bs2e_handle *h, int64_t *count);
 BS2E_API bs2e_status bs2e_synchronize(bs2e_handle *h);

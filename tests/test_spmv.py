@@ -157,6 +157,7 @@ def test_gpu_mv_on_device_blocks(bs2e, oracle):
                           {k: v.data_ptr() for k, v in Sd.items()}, on_device=True)
         xd = torch.from_numpy(x).to(dev)
         yd = torch.empty(n, dtype=torch.complex128, device=dev)
+        torch.cuda.synchronize()  # x was copied on torch's stream; the library uses its own
         h.csr_mv_device(0, n, n, nH, Hd["index_ptr"].data_ptr(), Hd["indices"].data_ptr(),
                         Hd["data"].data_ptr(), xd.data_ptr(), yd.data_ptr())
         y = yd.cpu().numpy()
@@ -229,6 +230,7 @@ def test_gpu_mv_columns_8_byte_aligned(bs2e, oracle):
             dat = torch.from_numpy(A["data"]).to(dev)
             xd = torch.from_numpy(x).to(dev)
             yd = torch.empty(200, dtype=torch.complex128, device=dev)
+            torch.cuda.synchronize()  # inputs copied on torch's stream
             h.csr_mv_device(0, 200, 150, A["nnz"], ptr.data_ptr(), idx.data_ptr(),
                             dat.data_ptr(), xd.data_ptr(), yd.data_ptr())
             _check(yd.cpu().numpy(), want, scale)
