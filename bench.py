@@ -697,6 +697,7 @@ def run_matvec(args):
                 y = torch.empty(n, dtype=torch.complex128, device=dev)
                 args_ = (op, n, n, nH, ptr.data_ptr(), idx.data_ptr(), dat.data_ptr(),
                          x.data_ptr(), y.data_ptr())
+                torch.cuda.synchronize()  # x is made on torch's stream, read on the library's
                 for _ in range(args.warmup):
                     h.csr_mv_device(*args_)
                 e0 = torch.cuda.Event(enable_timing=True)
