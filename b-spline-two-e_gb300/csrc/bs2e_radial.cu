@@ -131,7 +131,7 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
     double *sO = sRp + q * q;     // [k2][q]
     double *sJ = sO + k2 * q;     // [k2][q]
     double *sPk = sJ + k2 * q;    // [q] r^kk
-    double *sPm = sPk + q;        // [q] r^(kk+1)
+    double *sPm = sPk + q;        // [q] 1 / r^(kk+1)
     double *sW = sPm + q;         // [q]
     for (int e = threadIdx.x; e < kq; e += blockDim.x) sB[e] = tab_B[(size_t)iv * kq + e];
     for (int e = threadIdx.x; e < q * kq; e += blockDim.x) sBi[e] = tab_Bi[(size_t)iv * q * kq + e];
@@ -141,7 +141,9 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
         double r = tab_r[(size_t)iv * q + e];
         sR[e] = r;
         sPk[e] = powi(r, kk);
-        sPm[e] = powi(r, kk + 1);
+        // one division per point; the sums below multiply by it (within a
+        // rounding of dividing each term, far inside the parity bars)
+        sPm[e] = 1.0 / powi(r, kk + 1);
         sW[e] = glw[e];
     }
     __syncthreads();
@@ -154,7 +156,7 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
         for (int P = 0; P < q; ++P) {
             double wbb = sW[P] * sB[P * k + s1] * sB[P * k + s2];
             a = a + wbb * sPk[P];
-            b = b + wbb / sPm[P];
+            b = b + wbb * sPm[P];
         }
         mom[mbase + e] = h * a;
         mom[mbase + k2 + e] = h * b;
@@ -162,7 +164,7 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
     for (int e = threadIdx.x; e < k2 * q; e += blockDim.x) {
         int p = e / q, P = e - p * q;
         int si = p / k, sip = p - si * k;
-        sO[e] = sW[P] * sB[P * k + si] * sB[P * k + sip] / sPm[P];
+        sO[e] = sW[P] * sB[P * k + si] * sB[P * k + sip] * sPm[P];
         int sj = si, sjp = sip;
         double hP = 0.5 * (sR[P] - lo);
         double acc = 0.0;
