@@ -284,6 +284,7 @@ struct FillArgs {
     const double2 *Hb, *Sb;
     const float4 *Hbf, *Sbf;  // the same bands as FP32 pairs (re hi, re lo, im hi, im lo)
     int s_real;
+    int gated;                // 1: some channel pair needs the per-entry r_12_allowed test
     int ff_one_body;          // 1: mixed path may use Hbf/Sbf (S real, magnitudes in range)
     // rows [row0, row1) are filled; row r starts at output position
     // Hptr[r - ptr_row0] - 1 - Hbase (likewise S), 1-based CSR pointers
@@ -626,7 +627,14 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
                 }
                 const int excl = incl - cnt;
                 const int tot = __shfl_sync(FULL, incl, 31);
-                if (!MIXED && F.s_real) {
+                // The reference adds an entry's multipole sums only where
+                // r_12_allowed holds (a weight above 5e-15 under sup or sup_x;
+                // the sums keep weights above 5e-16).  Unless some pair of the
+                // block is flagged (PairInfo bit4: a term whose listed weights
+                // are all at most 5e-15; exact 3j/6j values give none),
+                // "under sup" alone decides and the two-entry loop needs no
+                // per-entry test; a flagged block takes the gated loop below.
+                if (!MIXED && F.s_real && !F.gated) {
                     // FP64 with a real S: two entries per lane (e and e + 32 of
                     // each 64), so the two run searches and the two multipole
                     // FMA chains are independent and overlap; an entry outside
@@ -1173,6 +1181,7 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     F.Hbf = h->d_Hbf;
     F.Sbf = h->d_Sbf;
     F.s_real = h->s_real ? 1 : 0;
+    F.gated = h->plan.gated ? 1 : 0;
     F.ff_one_body = h->ff_one_body ? 1 : 0;
     F.Hptr = d_Hptr;
     F.Sptr = d_Sptr;

@@ -65,6 +65,7 @@ void plan_channels(BlockPlan &P, int K1) {
     P.pair_a.assign((size_t)nc * nc * 2 * K1, 0.0);
     P.pair_af.assign((size_t)nc * nc * 2 * K1 * 2, 0.0f);
     const double exsign = P.spin ? -1.0 : 1.0;
+    P.gated = false;
     for (int r = 0; r < nc; ++r)
         for (int c = 0; c < nc; ++c) {
             int la = P.ch_l1[r], lb = P.ch_l2[r], lc = P.ch_l1[c], ld = P.ch_l2[c];
@@ -98,7 +99,13 @@ void plan_channels(BlockPlan &P, int K1) {
             }
             bool leq = (la == lc) && (lb == ld);
             bool leqx = (la == ld) && (lb == lc);
-            pi.flags = (dir_ok ? 1 : 0) | (ex_ok ? 2 : 0) | (leq ? 4 : 0) | (leqx ? 8 : 0);
+            // bit4: a listed weight lies in (5e-16, 5e-15] where no weight of that
+            // term passes 5e-15, so whether the sums apply depends per entry on
+            // the reference's r_12_allowed (the fill takes its gated path)
+            const bool gated = (!dir_ok && nd > 0) || (!ex_ok && nx > 0);
+            pi.flags = (dir_ok ? 1 : 0) | (ex_ok ? 2 : 0) | (leq ? 4 : 0) | (leqx ? 8 : 0) |
+                       (gated ? 16 : 0);
+            P.gated = P.gated || gated;
             pi.nd = nd;
             pi.nx = nx;
             pi.sgn = sgn;

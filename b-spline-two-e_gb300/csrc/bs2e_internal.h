@@ -36,7 +36,7 @@ constexpr int kRkBias = 112;
 
 // Per (row channel, column channel) coupling of one symmetry block.
 struct PairInfo {
-    int32_t flags;   // bit0 dir_ok, bit1 ex_ok, bit2 l_eq, bit3 l_eq_ex
+    int32_t flags;   // bit0 dir_ok, bit1 ex_ok, bit2 l_eq, bit3 l_eq_ex, bit4 sums gated per entry
     int32_t nd, nx;  // lengths of the direct / exchange multipole lists
     int32_t pad;
     double sgn;      // exchange sign (-1)^(l_c+l_d+L) (times -1 for the triplet)
@@ -58,6 +58,7 @@ struct BlockPlan {
     std::vector<int8_t> pair_k;               // [n_ch][n_ch][2][K1]
     std::vector<double> pair_a;               // [n_ch][n_ch][2][K1]
     std::vector<float> pair_af;               // [n_ch][n_ch][2][K1][2] (hi, lo) for the mixed path
+    bool gated = false;                       // some pair has PairInfo bit4 set
 };
 
 // Device side of the counted block.  The configuration list itself is the
