@@ -1109,9 +1109,15 @@ static bs2e_status blocks_args_ok(int64_t n_blocks, const bs2e_config *const *co
     return BS2E_OK;
 }
 
+static void clear_error(bs2e_handle *h) {
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->err.clear();
+}
+
 static bs2e_status block_failed(bs2e_handle *h, int64_t i, bs2e_status st) {
     std::lock_guard<std::mutex> lk(h->mu);
-    h->err = "block " + std::to_string(i) + ": " + h->err;
+    h->err = "block " + std::to_string(i) + ": " +
+             (h->err.empty() ? "invalid argument (status " + std::to_string(st) + ")" : h->err);
     return st;
 }
 
@@ -1124,6 +1130,7 @@ BS2E_API bs2e_status bs2e_blocks_count_all(bs2e_handle *h, int64_t n_blocks,
         (n_blocks > 0 && (!nnz_H || !nnz_S)))
         return BS2E_ERR_ARG;
     for (int64_t i = 0; i < n_blocks; ++i) {
+        clear_error(h);
         const bs2e_status st = bs2e_block_count_ex(h, configs[i], n_config[i], L[i], spin[i], full,
                                                    &nnz_H[i], &nnz_S[i]);
         if (st != BS2E_OK) return block_failed(h, i, st);
@@ -1144,6 +1151,7 @@ BS2E_API bs2e_status bs2e_blocks_fill_all(bs2e_handle *h, int64_t n_blocks,
                           !S_indices || !S_data)))
         return BS2E_ERR_ARG;
     for (int64_t i = 0; i < n_blocks; ++i) {
+        clear_error(h);
         const bs2e_status st = bs2e_block_fill_ex(
             h, configs[i], n_config[i], L[i], spin[i], full, H_index_ptr[i], H_indices[i],
             H_data[i], S_index_ptr[i], S_indices[i], S_data[i], out_on_device);
