@@ -751,7 +751,8 @@ def run_reference(args):
         vals.append(last["value"])
     v = statistics.median(vals)
     return {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "R^k elements/s", "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "R^k elements/s",
+        "n_gpus": args.gpus, "gpus_used": 0,  # the run's N; the arm itself runs on host cores
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * last["t_full_s"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (deterministic knot grid, no dataset)",
