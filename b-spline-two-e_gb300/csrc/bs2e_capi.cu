@@ -536,6 +536,9 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
             st = (e == cudaErrorMemoryAllocation) ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA;
     };
     bad(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    // the allocation-free lookup's static array, reserved now rather than at
+    // its first call (a caller may have filled HBM by then)
+    bad(noalloc_prepare(h->device, true));
     size_t q = g.q, kk = g.k, niv = g.n_iv, K1 = g.K1;
     bad(dalloc(&h->d_knots, (size_t)n_knots));
     bad(dalloc(&h->d_glx, q));

@@ -188,6 +188,10 @@ void gauss_legendre(int q, double *x, double *w);
 // Angular tables of a block from its ordered channel list.
 void plan_channels(BlockPlan &plan, int K1);
 
+// Scratch of the allocation-free R^k lookup (bs2e_noalloc.cu): resolves its
+// device address on `device` and loads its kernel (bs2e_create calls this).
+cudaError_t noalloc_prepare(int device, bool refresh);
+
 // Kernel launchers (bs2e_radial.cu)
 // Device view of one handle's radial buffers (the single-handle kernels and
 // the batched ones read the same struct).

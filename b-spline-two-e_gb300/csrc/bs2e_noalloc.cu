@@ -8,9 +8,15 @@
 // does the same lookup through one file-scope device array instead:
 //   - capacity kRkStaticMaxKeys keys per call (1.125 MiB per GPU that loads
 //     the library, held until the process exits);
-//   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (that device current); make that first call before
-//     any stream capture on the device;
+//   - bs2e_create resolves the array on the handle's device: it looks up the
+//     array's device address with cudaGetSymbolAddress (that device current)
+//     and loads the lookup kernel, so the module that holds the array is
+//     resident before the caller fills HBM (under lazy module loading the
+//     array would otherwise be reserved only at the first lookup).  The
+//     lookup itself repeats that set-up when it finds none for its device;
+//   - the address is valid for the device's current primary context: each
+//     bs2e_create looks it up again, and a handle does not outlive a
+//     cudaDeviceReset of its device;
 //   - every call on a device uses the same array and leaves its contents
 //     there: keys and values of the last call remain, nothing needs clearing
 //     because each call overwrites exactly the part it reads;
@@ -70,6 +76,24 @@ __global__ void k_rk_gather_static(const double *__restrict__ R, const float2 *_
 }
 
 }  // namespace
+
+// Looks up the scratch's device address on `device` (made current here) and
+// loads the lookup kernel; refresh = true repeats the lookup when an address
+// is cached already (a new handle may live in a new primary context).
+cudaError_t noalloc_prepare(int device, bool refresh) {
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> g(g_mu);
+    if (g_addr[device] && !refresh) return cudaSuccess;
+    cudaError_t e = cudaSetDevice(device);
+    void *p = nullptr;
+    if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_rk_scratch);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_rk_gather_static);
+    if (e == cudaSuccess && !p) e = cudaErrorInvalidSymbol;
+    g_addr[device] = (e == cudaSuccess) ? p : nullptr;
+    return e;
+}
+
 }  // namespace bs2e
 
 using namespace bs2e;
@@ -88,19 +112,21 @@ extern "C" BS2E_API bs2e_status bs2e_rk_get_batch_static(bs2e_handle *h, int64_t
         h->err = "bs2e_rk has not run";
         return BS2E_ERR_STATE;
     }
-    if (n == 0) return BS2E_OK;
     if (h->device < 0 || h->device >= 64) {
         h->err = "device ordinal out of range for the static scratch";
         return BS2E_ERR_ARG;
     }
+    // set up (normally done by bs2e_create) before the n == 0 return, so an
+    // empty call also leaves the array resolved
     cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = noalloc_prepare(h->device, false);
     void *base = nullptr;
     if (e == cudaSuccess) {
         std::lock_guard<std::mutex> g(g_mu);
-        if (!g_addr[h->device]) e = cudaGetSymbolAddress(&g_addr[h->device], g_rk_scratch);
         base = g_addr[h->device];
+        if (!base) e = cudaErrorInvalidSymbol;
     }
-    if (e == cudaSuccess && !base) e = cudaErrorInvalidSymbol;
+    if (e == cudaSuccess && n == 0) return BS2E_OK;
     int64_t *d_keys = (int64_t *)base;
     double *d_vals = (double *)((unsigned char *)base + kKeyBytes);
     const Radial &g = h->g;
@@ -121,7 +147,7 @@ extern "C" BS2E_API bs2e_status bs2e_rk_get_batch_static(bs2e_handle *h, int64_t
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
         h->err = std::string("bs2e_rk_get_batch_static: ") + cudaGetErrorString(e);
-        return BS2E_ERR_CUDA;
+        return e == cudaErrorMemoryAllocation ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA;
     }
     return BS2E_OK;
 }

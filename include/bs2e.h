@@ -137,10 +137,15 @@ BS2E_API bs2e_status bs2e_rk_export(bs2e_handle *h, int64_t k, double *out, int6
  * for the whole device, stalling work on other streams.  Keys and values are
  * staged in one file-scope device array of at most 4096 keys (1.125 MiB on
  * every GPU that loads the library, held until the process exits); larger n
- * is rejected with BS2E_ERR_ARG.  The first call on a device looks up the
- * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture on that device.  All calls on a device share the array, which keeps
- * the last call's contents; calls whose GPU work overlaps race on it. */
+ * is rejected with BS2E_ERR_ARG.  bs2e_create reserves the array on the
+ * handle's device (it looks up the array's address with cudaGetSymbolAddress
+ * and loads the lookup kernel), so the array is resident before the caller
+ * fills HBM; if that set-up is missing for a device, the first call on it
+ * (n = 0 included) does it and should come before any stream capture there.
+ * The address holds for the device's current primary context; a handle does
+ * not survive cudaDeviceReset.  Allocation failures during set-up return
+ * BS2E_ERR_NOMEM.  All calls on a device share the array, which keeps the
+ * last call's contents; calls whose GPU work overlaps race on it. */
 BS2E_API bs2e_status bs2e_rk_get_batch_static(bs2e_handle *h, int64_t n, const int64_t *keys,
                                               double *vals);
 
