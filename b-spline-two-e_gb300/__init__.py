@@ -96,6 +96,9 @@ def lib():
         "bs2e_csr_from_blocks": (st, [p, i64, i64, p, p, p, p, p, p, p, p, i64]),
         "bs2e_block_count_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p]),
         "bs2e_block_fill_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, i64]),
+        "bs2e_block_band_count": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p]),
+        "bs2e_block_fill_band": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, p]),
+        "bs2e_set_block_cache": (st, [p, i64]),
         "bs2e_set_one_body": (st, [p, p, i64, p]),
         "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
         "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
@@ -366,6 +369,33 @@ class Bs2e:
                                                     int(row_count), ctypes.byref(nh),
                                                     ctypes.byref(ns)))
         return nh.value, ns.value
+
+    def band_count(self, cf, L, n1_first, n1_count, full=True, spin=0, per_n1=False):
+        """(rows, nnz_H, nnz_S) of the n1 band [n1_first, n1_first + n1_count)
+        of a block; with per_n1 also an (n1_count, 3) array of the same per n1."""
+        cf = as_configs(cf)
+        r, nh, ns = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        per = np.zeros((int(n1_count), 3), dtype=np.int64) if per_n1 else None
+        _check(self._h, lib().bs2e_block_band_count(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                    int(bool(full)), int(n1_first), int(n1_count),
+                                                    ctypes.byref(r), ctypes.byref(nh),
+                                                    ctypes.byref(ns), _ptr(per)))
+        return (r.value, nh.value, ns.value, per) if per_n1 else (r.value, nh.value, ns.value)
+
+    def band_into(self, cf, L, n1_first, n1_count, full, spin, H, S, rows=None):
+        """Band fill into device buffers (dicts of integer device addresses;
+        rows: device address for the 1-based block rows, or None)."""
+        cf = as_configs(cf)
+        args = [ctypes.c_void_p(int(H[x])) for x in ("index_ptr", "indices", "data")]
+        args += [ctypes.c_void_p(int(S[x])) for x in ("index_ptr", "indices", "data")]
+        rp = ctypes.c_void_p(int(rows)) if rows else None
+        _check(self._h, lib().bs2e_block_fill_band(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                   int(bool(full)), int(n1_first), int(n1_count),
+                                                   rp, *args))
+
+    def set_block_cache(self, n_blocks):
+        """Counted blocks kept besides the current one (0..16)."""
+        _check(self._h, lib().bs2e_set_block_cache(self._h, int(n_blocks)))
 
     def block_fill_into(self, cf, L, full, spin, H, S, on_device=False):
         """Fills caller-provided arrays: numpy (host) or, with on_device, integer

@@ -287,9 +287,12 @@ struct FillArgs {
     int gated;                // 1: some channel pair needs the per-entry r_12_allowed test
     int ff_one_body;          // 1: mixed path may use Hbf/Sbf (S real, magnitudes in range)
     // rows [row0, row1) are filled; row r starts at output position
-    // Hptr[r - ptr_row0] - 1 - Hbase (likewise S), 1-based CSR pointers
+    // Hptr[x] - 1 - Hbase (likewise S), 1-based CSR pointers, where x is
+    // r - ptr_row0, or in a band fill band[n_ch + c] + (r - band[c]) for r in
+    // channel c
     const int64_t *Hptr, *Sptr;
     int64_t row0, row1, ptr_row0, Hbase, Sbase;
+    const int *band;
     int a0;  // tile (n_a, n_b) of CTA x: n_a = a0 + x / N, n_b = x % N + 1
     int64_t *Hidx, *Sidx;
     double2 *Hdat, *Sdat;
@@ -521,7 +524,7 @@ __device__ __forceinline__ double wide_sums(const float2 *R2, const int *sexp, c
 // per-multipole exponents at sexp (mixed store) and the warp's scratch for the
 // scaled multipole weights.
 template <bool MIXED>
-__device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const int c_r,
+__device__ __forceinline__ void fill_row(const FillArgs &F, const int local, const int c_r,
                                          const int n_a, const int n_b, const double *sR,
                                          const int *sexp, float2 (*sAw)[kMaxK1],
                                          int (*sKow)[kMaxK1]) {
@@ -540,8 +543,8 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int row, const
     const double2 *HaR = F.Hb + (size_t)l_a * A.N * W + ra;  // FP64 band rows, same indexing
     const double2 *HbR = F.Hb + (size_t)l_b * A.N * W + rb;
     const double2 *SaR = F.Sb + ra, *SbR = F.Sb + rb;
-    int64_t oH = F.Hptr[row - F.ptr_row0] - 1 - F.Hbase;
-    int64_t oS = F.Sptr[row - F.ptr_row0] - 1 - F.Sbase;
+    int64_t oH = F.Hptr[local] - 1 - F.Hbase;
+    int64_t oS = F.Sptr[local] - 1 - F.Sbase;
     for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
         const PairInfo pi = A.pairs[(size_t)c_r * A.n_ch + c_c];
         const int flags = pi.flags;
@@ -1018,7 +1021,8 @@ __global__ void __launch_bounds__(128, MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_
     const BlockArgs &A = F.B;
     const int n_a = F.a0 + (int)(blockIdx.x / A.N), n_b = blockIdx.x % A.N + 1;
     const size_t tix = (size_t)(n_a - 1) * A.N + (n_b - 1);
-    // rows of this tile: one per channel whose (n1 = n_a) group holds n2 = n_b
+    // rows of this tile: one per channel whose (n1 = n_a) group holds n2 = n_b;
+    // srow keeps each row's output index (its pointer slot)
     if (threadIdx.x == 0) snrow = 0;
     __syncthreads();
     for (int c = threadIdx.x; c < A.n_ch; c += blockDim.x) {
@@ -1027,7 +1031,8 @@ __global__ void __launch_bounds__(128, MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_
         const int64_t row = base + (n_b - lo);
         if (base >= 0 && lo <= n_b && n_b <= hi && row >= F.row0 && row < F.row1) {
             int slot = atomicAdd(&snrow, 1);
-            srow[slot] = (int)row;
+            srow[slot] = F.band ? F.band[A.n_ch + c] + (int)(row - F.band[c])
+                                : (int)(row - F.ptr_row0);
             sch[slot] = c;
         }
     }
@@ -1066,7 +1071,46 @@ __global__ void __launch_bounds__(128, 6) k_csr_fill_rows(FillArgs F) {
         for (int i = lane; i < A.K1; i += 32) sexpw[warp][i] = F.Rexp[tix * A.K1 + i];
         __syncwarp();
     }
-    fill_row<MIXED>(F, (int)row, c_r, n_a, n_b, R, sexpw[warp], sA[warp], sKo[warp]);
+    fill_row<MIXED>(F, (int)(row - F.ptr_row0), c_r, n_a, n_b, R, sexpw[warp], sA[warp],
+                    sKo[warp]);
+}
+
+__global__ void k_gather_i64(const int64_t *__restrict__ src, const int64_t *__restrict__ idx,
+                             int64_t n, int64_t *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = src[idx[i]];
+}
+
+// Band-local pointers: local row i lies in the channel c with the largest
+// local offset band[n_ch + c] <= i (channels without band rows share their
+// successor's offset), at block row band[c] + (i - band[n_ch + c]).
+__global__ void k_band_ptr(const int *__restrict__ band, const int64_t *__restrict__ boff,
+                           int n_ch, int64_t n_rows, const int64_t *__restrict__ pfxH,
+                           const int64_t *__restrict__ pfxS, int64_t *__restrict__ Hptr,
+                           int64_t *__restrict__ Sptr, int64_t *__restrict__ rows) {
+    __shared__ int soff[kMaxCh];
+    for (int c = threadIdx.x; c < n_ch; c += blockDim.x) soff[c] = band[n_ch + c];
+    __syncthreads();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n_rows;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (i == n_rows) {
+            Hptr[i] = boff[n_ch] + 1;
+            Sptr[i] = boff[2 * n_ch + 1] + 1;
+            continue;
+        }
+        int lo = 0, hi = n_ch - 1;  // largest c with soff[c] <= i
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (soff[mid] <= i) lo = mid;
+            else hi = mid - 1;
+        }
+        const int c = lo;
+        const int64_t first = band[c], row = first + (i - soff[c]);
+        Hptr[i] = pfxH[row] - pfxH[first] + boff[c] + 1;
+        Sptr[i] = pfxS[row] - pfxS[first] + boff[n_ch + 1 + c] + 1;
+        if (rows) rows[i] = row + 1;
+    }
 }
 
 }  // namespace
@@ -1196,6 +1240,7 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     F.Hbase = r.Hbase;
     F.Sbase = r.Sbase;
     F.a0 = r.a0;
+    F.band = r.band;
     size_t smem = fill_smem(h->g);
     if (h->plan.n_config > 0 && r.row1 > r.row0 && r.rows_mode) {
         const unsigned grid = (unsigned)((r.row1 - r.row0 + 3) / 4);
@@ -1217,6 +1262,25 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
         }
         h->launches++;
     }
+}
+
+}  // namespace bs2e
+
+namespace bs2e {
+
+void launch_gather_i64(bs2e_handle *h, const int64_t *src, const int64_t *idx, int64_t n,
+                       int64_t *out) {
+    if (n <= 0) return;
+    k_gather_i64<<<grid_rows(n), 256, 0, h->stream>>>(src, idx, n, out);
+    h->launches++;
+}
+
+void launch_band_ptr(bs2e_handle *h, const int *band, const int64_t *boff, int n_ch,
+                     int64_t n_rows, int64_t *Hptr, int64_t *Sptr, int64_t *rows) {
+    k_band_ptr<<<grid_rows(n_rows + 1), 256, 0, h->stream>>>(band, boff, n_ch, n_rows,
+                                                             h->blk.pfxH, h->blk.pfxS, Hptr,
+                                                             Sptr, rows);
+    h->launches++;
 }
 
 }  // namespace bs2e

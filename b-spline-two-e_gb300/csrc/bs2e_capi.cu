@@ -90,6 +90,10 @@ void free_block(DevBlock &b) {
     dfree(b.cntS);
     dfree(b.scan_tmp);
     dfree(b.stats);
+    dfree(b.pfxH);
+    dfree(b.pfxS);
+    b.pfx_cap = 0;
+    b.pfx_valid = false;
     b.cfg_cap = b.cfg_new_cap = b.seg_cap = b.pair_cap = b.cntH_cap = b.cntS_cap = b.scan_cap = 0;
     b.nnzH = b.nnzS = -1;
     b.valid = false;
@@ -163,7 +167,7 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
         h->plan = e.second;
         return BS2E_OK;
     }
-    if (h->blk.valid) {
+    if (h->blk.valid && h->cache_max > 0) {
         // park the current block; the upload moves to a fresh one
         DevBlock nb;
         std::swap(nb.cfg_new, h->blk.cfg_new);
@@ -174,7 +178,7 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
         size_t keep = 0;
         for (; keep < h->parked.size(); ++keep) {
             rows += h->parked[keep].first.n;
-            if (keep >= (size_t)kBlockCache || rows > kBlockCacheRows) break;
+            if (keep >= (size_t)h->cache_max || rows > kBlockCacheRows) break;
         }
         while (h->parked.size() > keep) {
             free_block(h->parked.back().first);
@@ -188,6 +192,7 @@ bs2e_status ensure_counted(bs2e_handle *h, const bs2e_config *cf, int64_t n_conf
     if (!B.chl) CU(dalloc(&B.chl, kMaxCh));
     CU(cudaMemsetAsync(B.stats, 0, 8 * sizeof(unsigned long long), h->stream));
     B.valid = false;
+    B.pfx_valid = false;
     BlockPlan &P = h->plan;
     P = BlockPlan();
     P.n_config = n_config;
@@ -599,6 +604,9 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_dip_part);
         dfree(h->d_rptrH);
         dfree(h->d_rptrS);
+        dfree(h->d_band);
+        dfree(h->d_band_idx);
+        dfree(h->d_band_val);
         dfree(h->d_stage[0]);
         dfree(h->d_stage[1]);
         if (h->copy_stream) cudaStreamSynchronize(h->copy_stream), cudaStreamDestroy(h->copy_stream);
@@ -1216,6 +1224,182 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
                       (double2 *)S_data);
     CU(cudaGetLastError());
     return sync_check(h, "block fill (rows)");
+}
+
+// 1-based CSR pointers of the whole counted block (a scan of its row
+// counts), built once per counted block for band fills.
+static bs2e_status ensure_prefix(bs2e_handle *h) {
+    DevBlock &B = h->blk;
+    if (B.pfx_valid) return BS2E_OK;
+    const int64_t n = h->plan.n_config;
+    if (n + 1 > B.pfx_cap) {
+        dfree(B.pfxH);
+        dfree(B.pfxS);
+        B.pfx_cap = 0;
+        CU(dalloc(&B.pfxH, (size_t)n + 1));
+        CU(dalloc(&B.pfxS, (size_t)n + 1));
+        B.pfx_cap = n + 1;
+    }
+    launch_block_scan(h, B.pfxH, B.pfxS, 0, n);
+    CU(cudaGetLastError());
+    B.pfx_valid = true;
+    return BS2E_OK;
+}
+
+// Band boundaries of the counted block: rows[c * (nx + 1) + j] is the first
+// row of channel c with n1 >= x0 + j (j = 0..nx; channel c holds rows
+// [ch_start[c], ch_start[c + 1])), PH / PS the block's 1-based pointers there.
+static bs2e_status band_bounds(bs2e_handle *h, const bs2e_config *cf, int64_t x0, int64_t nx,
+                               std::vector<int64_t> &rows, std::vector<int64_t> &PH,
+                               std::vector<int64_t> &PS) {
+    const BlockPlan &P = h->plan;
+    const int n_ch = P.n_ch;
+    const int64_t m = (int64_t)n_ch * (nx + 1);
+    rows.assign((size_t)m, 0);
+    for (int c = 0; c < n_ch; ++c) {
+        const int64_t lo = P.ch_start[c], hi = c + 1 < n_ch ? P.ch_start[c + 1] : P.n_config;
+        int64_t r = lo;
+        for (int64_t j = 0; j <= nx; ++j) {
+            // n1 ascends within a channel (checked when the block was counted)
+            int64_t a = r, b = hi;
+            while (a < b) {
+                const int64_t mid = a + (b - a) / 2;
+                if (cf[mid].n1 < x0 + j) a = mid + 1;
+                else b = mid;
+            }
+            r = a;
+            rows[(size_t)c * (nx + 1) + j] = r;
+        }
+    }
+    PH.assign((size_t)m, 1);
+    PS.assign((size_t)m, 1);
+    if (m == 0) return BS2E_OK;
+    TRY(ensure_prefix(h));
+    if (2 * m > h->band_cap || !h->d_band_idx) {
+        dfree(h->d_band_idx);
+        dfree(h->d_band_val);
+        h->band_cap = 0;
+        const int64_t cap = std::max<int64_t>(2 * m, 2 * (kMaxCh + 1));
+        CU(dalloc(&h->d_band_idx, (size_t)cap));
+        CU(dalloc(&h->d_band_val, (size_t)cap));
+        h->band_cap = cap;
+    }
+    CU(cudaMemcpyAsync(h->d_band_idx, rows.data(), sizeof(int64_t) * m, cudaMemcpyHostToDevice,
+                       h->stream));
+    launch_gather_i64(h, h->blk.pfxH, h->d_band_idx, m, h->d_band_val);
+    launch_gather_i64(h, h->blk.pfxS, h->d_band_idx, m, h->d_band_val + m);
+    CU(cudaMemcpyAsync(PH.data(), h->d_band_val, sizeof(int64_t) * m, cudaMemcpyDeviceToHost,
+                       h->stream));
+    CU(cudaMemcpyAsync(PS.data(), h->d_band_val + m, sizeof(int64_t) * m,
+                       cudaMemcpyDeviceToHost, h->stream));
+    return sync_check(h, "band bounds");
+}
+
+BS2E_API bs2e_status bs2e_block_band_count(bs2e_handle *h, const bs2e_config *configs,
+                                           int64_t n_config, int64_t L, int64_t spin,
+                                           int64_t full, int64_t n1_first, int64_t n1_count,
+                                           int64_t *n_rows, int64_t *nnz_H, int64_t *nnz_S,
+                                           int64_t *per_n1) {
+    if (!h || n_config < 0 || !n_rows || !nnz_H || !nnz_S || n1_count < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    if (n1_count > (int64_t)1 << 24) return fail(h, BS2E_ERR_ARG, "n1_count too large");
+    TRY(ensure_counted(h, configs, n_config, L, spin, full));
+    std::vector<int64_t> rows, PH, PS;
+    const int64_t nx = per_n1 ? n1_count : 1;
+    TRY(band_bounds(h, configs, n1_first, nx, rows, PH, PS));
+    const int n_ch = h->plan.n_ch;
+    int64_t r = 0, eh = 0, es = 0;
+    if (per_n1) memset(per_n1, 0, sizeof(int64_t) * 3 * (size_t)n1_count);
+    for (int c = 0; c < n_ch; ++c) {
+        const size_t o = (size_t)c * (nx + 1);
+        r += rows[o + nx] - rows[o];
+        eh += PH[o + nx] - PH[o];
+        es += PS[o + nx] - PS[o];
+        if (per_n1)
+            for (int64_t j = 0; j < nx; ++j) {
+                per_n1[3 * j] += rows[o + j + 1] - rows[o + j];
+                per_n1[3 * j + 1] += PH[o + j + 1] - PH[o + j];
+                per_n1[3 * j + 2] += PS[o + j + 1] - PS[o + j];
+            }
+    }
+    *n_rows = r;
+    *nnz_H = eh;
+    *nnz_S = es;
+    return BS2E_OK;
+}
+
+BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *configs,
+                                          int64_t n_config, int64_t L, int64_t spin,
+                                          int64_t full, int64_t n1_first, int64_t n1_count,
+                                          int64_t *rows_out, int64_t *H_index_ptr,
+                                          int64_t *H_indices, double *H_data,
+                                          int64_t *S_index_ptr, int64_t *S_indices,
+                                          double *S_data) {
+    if (!h || n_config < 0 || n1_count < 0) return BS2E_ERR_ARG;
+    Guard G(h);
+    TRY(fill_ready(h, configs, n_config, L, spin, full));
+    std::vector<int64_t> rows, PH, PS;
+    TRY(band_bounds(h, configs, n1_first, 1, rows, PH, PS));
+    const int n_ch = h->plan.n_ch;
+    std::vector<int> band(2 * (size_t)std::max(n_ch, 1), 0);
+    std::vector<int64_t> boff(2 * ((size_t)n_ch + 1), 0);
+    int64_t nr = 0;
+    for (int c = 0; c < n_ch; ++c) {
+        band[c] = (int)rows[2 * c];
+        band[n_ch + c] = (int)nr;
+        nr += rows[2 * c + 1] - rows[2 * c];
+        boff[c + 1] = boff[c] + (PH[2 * c + 1] - PH[2 * c]);
+        boff[n_ch + 2 + c] = boff[n_ch + 1 + c] + (PS[2 * c + 1] - PS[2 * c]);
+    }
+    const int64_t nH = boff[n_ch], nS = boff[2 * n_ch + 1];
+    if (!H_index_ptr || !S_index_ptr || (nH > 0 && (!H_indices || !H_data)) ||
+        (nS > 0 && (!S_indices || !S_data)))
+        return fail(h, BS2E_ERR_ARG, "NULL output array");
+    if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
+        !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16) ||
+        !aligned(rows_out, 8))
+        return fail(h, BS2E_ERR_ARG, "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
+    if (!h->d_band) CU(dalloc(&h->d_band, (size_t)2 * kMaxCh));
+    if (!h->d_band_val) {
+        CU(dalloc(&h->d_band_idx, (size_t)2 * (kMaxCh + 1)));
+        CU(dalloc(&h->d_band_val, (size_t)2 * (kMaxCh + 1)));
+        h->band_cap = 2 * (kMaxCh + 1);
+    }
+    CU(cudaMemcpyAsync(h->d_band, band.data(), sizeof(int) * 2 * n_ch, cudaMemcpyHostToDevice,
+                       h->stream));
+    CU(cudaMemcpyAsync(h->d_band_val, boff.data(), sizeof(int64_t) * boff.size(),
+                       cudaMemcpyHostToDevice, h->stream));
+    launch_band_ptr(h, h->d_band, h->d_band_val, n_ch, nr, H_index_ptr, S_index_ptr, rows_out);
+    const int64_t a0 = std::max<int64_t>(n1_first, 1),
+                  a1 = std::min<int64_t>(n1_first + n1_count - 1, h->g.N);
+    if (nr > 0 && a1 >= a0) {
+        FillRange r;
+        r.row0 = 0;
+        r.row1 = n_config;
+        r.a0 = (int)a0;
+        r.a1 = (int)a1;
+        r.band = h->d_band;
+        launch_block_fill(h, r, H_index_ptr, S_index_ptr, H_indices, (double2 *)H_data,
+                          S_indices, (double2 *)S_data);
+    }
+    CU(cudaGetLastError());
+    return sync_check(h, "block fill (band)");
+}
+
+BS2E_API bs2e_status bs2e_set_block_cache(bs2e_handle *h, int64_t n_blocks) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard G(h);
+    if (n_blocks < 0 || n_blocks > kBlockCache)
+        return fail(h, BS2E_ERR_ARG, "block cache size must be 0..16");
+    h->cache_max = (int)n_blocks;
+    if (h->parked.size() > (size_t)n_blocks) {
+        CU(cudaStreamSynchronize(h->stream));
+        while (h->parked.size() > (size_t)n_blocks) {
+            free_block(h->parked.back().first);
+            h->parked.pop_back();
+        }
+    }
+    return BS2E_OK;
 }
 
 BS2E_API bs2e_status bs2e_block_fill(bs2e_handle *h, const bs2e_config *configs,

@@ -83,6 +83,11 @@ struct DevBlock {
     int64_t scan_cap = 0;
     unsigned long long *stats = nullptr;  // [0] error bits, [1..2] count_nnz H,S, [3..4] construct H,S, [5] marks
     int64_t nnzH = -1, nnzS = -1;
+    // 1-based CSR pointers of the whole block (n + 1 each), built on demand
+    // for band fills and kept with the block
+    int64_t *pfxH = nullptr, *pfxS = nullptr;
+    int64_t pfx_cap = 0;
+    bool pfx_valid = false;
     // identity of the counted block
     bool valid = false;
     int64_t L = -1, spin = -1, full = -1, n = -1;
@@ -149,6 +154,11 @@ struct bs2e_handle {
     bs2e::BlockPlan plan;
     bs2e::DevBlock blk;
     std::vector<std::pair<bs2e::DevBlock, bs2e::BlockPlan>> parked;
+    int cache_max = bs2e::kBlockCache;  // parked blocks kept (bs2e_set_block_cache)
+    // band fills: per channel (first row, local row offset) and gather scratch
+    int *d_band = nullptr;
+    int64_t *d_band_idx = nullptr, *d_band_val = nullptr;
+    int64_t band_cap = 0;
     // radial dipole bands (M1, M2) and dipole-block work buffers
     double2 *d_dM1 = nullptr, *d_dM2 = nullptr;
     int dip_gauge = -1;
@@ -262,11 +272,23 @@ void scan_one(bs2e_handle *h, const int64_t *in, int64_t n, int64_t *part, int64
 // rows_mode: a warp per row with the R^k tile read through L1/L2 (ranges
 // inside one or two channels, where each tile holds a single row of the
 // range) instead of a CTA per staged tile.
+// band (device, 2 x n_ch ints, or null): a band fill, where row r of channel
+// c is local row band[n_ch + c] + (r - band[c]) of the output, whose pointers
+// start at ptr[0] = 1.
 struct FillRange {
     int64_t row0 = 0, row1 = 0, ptr_row0 = 0, Hbase = 0, Sbase = 0;
     int a0 = 1, a1 = 0;
     bool rows_mode = false;
+    const int *band = nullptr;
 };
+// out[i] = src[idx[i]] for i < n (device arrays)
+void launch_gather_i64(bs2e_handle *h, const int64_t *src, const int64_t *idx, int64_t n,
+                       int64_t *out);
+// Band-local 1-based pointers of a band of n_rows rows: band (device, 2 x n_ch
+// ints as in FillRange) and boff (device, 2 x n_ch int64: H and S non-zeros of
+// the band before channel c); rows (may be null) gets the 1-based block rows.
+void launch_band_ptr(bs2e_handle *h, const int *band, const int64_t *boff, int n_ch,
+                     int64_t n_rows, int64_t *Hptr, int64_t *Sptr, int64_t *rows);
 // 1-based CSR pointers of rows [row0, row0 + n) (n + 1 entries, starting at 1)
 void launch_block_scan(bs2e_handle *h, int64_t *d_Hptr, int64_t *d_Sptr, int64_t row0,
                        int64_t n);

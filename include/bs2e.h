@@ -315,6 +315,43 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
                                           int64_t *S_indices, double *S_data,
                                           int64_t out_on_device);
 
+/* n1 bands of a block, for consumers that take a block piece by piece on the
+ * device (config lists of 10^7 rows, terabytes of CSR): the band holds the
+ * rows of EVERY channel whose n1 lies in [n1_first, n1_first + n1_count), in
+ * block order (channel by channel).  Unlike a contiguous row range, whose rows
+ * (n1, n2) each need their own R^k tile, a band gives every staged tile
+ * (n_a, n_b) the rows of all channels that read it, as the whole-block fill
+ * does.  band_count returns the band's row and non-zero counts and, when
+ * per_n1 != NULL, per n1 of the range the triple (rows, nnz_H, nnz_S) in
+ * per_n1[3*i .. 3*i+2] (for choosing bands that fit a buffer).  fill_band
+ * writes the band's CSR (range-local 1-based index_ptr, n_rows + 1 entries;
+ * the block's 1-based column indices) into DEVICE arrays on the handle's
+ * device, and, when rows != NULL (device, n_rows entries), the 1-based block
+ * row of every band row.  The same configuration list, L, spin and full as
+ * bs2e_block_count_ex.  No counterpart in the reference (its blocks are built
+ * whole, hamiltonian.f90:106-283). */
+BS2E_API bs2e_status bs2e_block_band_count(bs2e_handle *h, const bs2e_config *configs,
+                                           int64_t n_config, int64_t L, int64_t spin,
+                                           int64_t full, int64_t n1_first, int64_t n1_count,
+                                           int64_t *n_rows, int64_t *nnz_H, int64_t *nnz_S,
+                                           int64_t *per_n1);
+BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *configs,
+                                          int64_t n_config, int64_t L, int64_t spin,
+                                          int64_t full, int64_t n1_first, int64_t n1_count,
+                                          int64_t *rows, int64_t *H_index_ptr,
+                                          int64_t *H_indices, double *H_data,
+                                          int64_t *S_index_ptr, int64_t *S_indices,
+                                          double *S_data);
+
+/* How many counted blocks the handle keeps besides the current one (0..16;
+ * 16 at creation).  A kept block is reused when the same configuration list
+ * is counted or filled again, skipping its planning and count pass; with 0
+ * every block other than the last one counted is planned and counted anew,
+ * as count_nnz runs once per block in basis_setup (hamiltonian.f90:348-416),
+ * on the same device buffers.  Lowering the number frees the blocks beyond
+ * it.  No counterpart in the reference. */
+BS2E_API bs2e_status bs2e_set_block_cache(bs2e_handle *h, int64_t n_blocks);
+
 /* Product of a 1-based CSR matrix (n_rows x n_cols, nnz entries, complex128
  * data) with a complex128 vector, as the solvers apply H and S:
  *   op 0: y = A x             CSR_mv     (src/tools/sparse_array_tools.f90:966-994)

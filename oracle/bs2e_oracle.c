@@ -429,6 +429,190 @@ void or_rk_map(int64_t n_b, int64_t k, int64_t max_k, int64_t nnz4, const double
 }
 
 /* ------------------------------------------------------------------------ */
+/* R^k of selected tiles, for bases where the full primitives are too slow    */
+/* ------------------------------------------------------------------------ */
+
+/* Spline values of one breakpoint interval at or_slater's quadrature points:
+ * outer radii r[s] and, for each s, the inner radii rj[s][u] of the kink-split
+ * integral on [lo, r[s]]; B[s][f] / Bj[s][u][f] hold full spline ir + f
+ * (f < k), the only ones non-zero on the interval.  Same expressions as
+ * or_slater, so every cached value is the one or_slater computes. */
+typedef struct {
+    int64_t ir;
+    double lo, hi;
+    double *r, *B, *rj, *Bj;
+} iv_cache;
+
+static void iv_cache_fill(iv_cache *c, const double *knots, int64_t n, int64_t k, int64_t q,
+                          const double *x, int64_t ir) {
+    const double *bp = knots + (k - 1);
+    c->ir = ir;
+    c->lo = bp[ir - 1];
+    c->hi = bp[ir];
+    double scale = 0.5 * (c->hi - c->lo), translate = 0.5 * (c->hi + c->lo);
+    for (int64_t s = 0; s < q; ++s) {
+        double rs = scale * x[s] + translate;
+        c->r[s] = rs;
+        for (int64_t f = 0; f < k; ++f) c->B[s * k + f] = or_bvalue(knots, n, k, rs, 0, ir, ir + f);
+        double scj = 0.5 * (rs - c->lo), trj = 0.5 * (rs + c->lo);
+        for (int64_t u = 0; u < q; ++u) {
+            double rj = scj * x[u] + trj;
+            c->rj[s * q + u] = rj;
+            for (int64_t f = 0; f < k; ++f)
+                c->Bj[(s * q + u) * k + f] = or_bvalue(knots, n, k, rj, 0, ir, ir + f);
+        }
+    }
+}
+
+/* Entry v of a tile's interval cache, filled on first use. */
+static const iv_cache *ivc_get(iv_cache *cache, double **mem, int64_t v, size_t per,
+                               const double *knots, int64_t n, int64_t k, int64_t q,
+                               const double *x, int64_t ir) {
+    iv_cache *c = &cache[v];
+    if (!mem[v]) {
+        double *m = (double *)malloc(sizeof(double) * per);
+        mem[v] = m;
+        c->r = m;
+        c->B = m + q;
+        c->rj = m + q + q * k;
+        c->Bj = m + q + q * k + q * q;
+        iv_cache_fill(c, knots, n, k, q, x, ir);
+    }
+    return c;
+}
+
+/* r_k / r_m_k of basis pair (ib, jb) on interval c->ir for multipole kk:
+ * compute_Slater_off_diag (mat_els.f90:392-439) as or_slater evaluates it. */
+static void prim_off(const iv_cache *c, int64_t k, int64_t q, const double *w, int64_t ib,
+                     int64_t jb, int64_t kk, double *rk, double *rmk) {
+    double scale = 0.5 * (c->hi - c->lo);
+    int64_t fi = ib + 1 - c->ir, fj = jb + 1 - c->ir;
+    double a = 0.0, b = 0.0;
+    for (int64_t s = 0; s < q; ++s) {
+        double Bi = c->B[s * k + fi], Bj = c->B[s * k + fj];
+        a = a + w[s] * Bi * Bj * powi(c->r[s], kk);
+        b = b + w[s] * Bi * Bj / powi(c->r[s], kk + 1);
+    }
+    *rk = scale * a;
+    *rmk = scale * b;
+}
+
+/* r_d_k of (ib, ibp; jb, jbp) on interval c->ir for multipole kk:
+ * compute_Slater_diag (mat_els.f90:441-491) as or_slater evaluates it. */
+static double prim_diag(const iv_cache *c, int64_t k, int64_t q, const double *w, int64_t ib,
+                        int64_t ibp, int64_t jb, int64_t jbp, int64_t kk) {
+    double sci = 0.5 * (c->hi - c->lo);
+    int64_t fi = ib + 1 - c->ir, fip = ibp + 1 - c->ir, fj = jb + 1 - c->ir,
+            fjp = jbp + 1 - c->ir;
+    double acc = 0.0;
+    for (int64_t s = 0; s < q; ++s) {
+        double scj = 0.5 * (c->r[s] - c->lo);
+        double intj = 0.0;
+        for (int64_t u = 0; u < q; ++u) {
+            const double *Bu = c->Bj + (s * q + u) * k;
+            intj = intj + w[u] * Bu[fj] * Bu[fjp] * powi(c->rj[s * q + u], kk);
+        }
+        intj = scj * intj;
+        acc = acc + w[s] * c->B[s * k + fi] * c->B[s * k + fip] * intj / powi(c->r[s], kk + 1);
+    }
+    return sci * acc;
+}
+
+/* Intervals (1-based, ascending) where basis splines i and j are both
+ * non-zero: support(ir, i+1) and support(ir, j+1), clipped to 1..n_iv. */
+static void pair_ivs(int64_t i, int64_t j, int64_t k, int64_t n_iv, int64_t *lo, int64_t *hi) {
+    int64_t mx = i > j ? i : j, mn = i < j ? i : j;
+    *lo = mx + 2 - k < 1 ? 1 : mx + 2 - k;
+    *hi = mn + 1 > n_iv ? n_iv : mn + 1;
+}
+
+void or_rk_tiles(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL, int64_t max_k,
+                 int64_t n_tiles, const int64_t *ab, double *out, int nthreads) {
+    int64_t n = n_knots - k, nb = n - 2, n_iv = n_knots - 2 * k + 1;
+    int64_t K1 = max_k + 1, W = 2 * k - 1, q = k_GL;
+    double x[64], w[64];
+    or_gauss_legendre(q, x, w);
+    if (nthreads <= 0) {
+#ifdef _OPENMP
+        nthreads = omp_get_max_threads();
+#else
+        nthreads = 1;
+#endif
+    }
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int64_t t = 0; t < n_tiles; ++t) {
+        const int64_t a = ab[2 * t], b = ab[2 * t + 1];
+        double *o = out + (size_t)t * W * W * K1;
+        memset(o, 0, sizeof(double) * (size_t)W * W * K1);
+        /* intervals the pairs (a, c) and (b, d) of the tile can share:
+         * [a + 2 - k, a + 1] and [b + 2 - k, b + 1], filled on first use */
+        int64_t lo = (a < b ? a : b) + 2 - k, hi = (a > b ? a : b) + 1;
+        if (lo < 1) lo = 1;
+        if (hi > n_iv) hi = n_iv;
+        int64_t niv = hi - lo + 1;
+        const size_t per = (size_t)(q + q * k + q * q + q * q * k);
+        iv_cache *cache = (iv_cache *)calloc((size_t)niv, sizeof(iv_cache));
+        double **mem = (double **)calloc((size_t)niv, sizeof(double *));
+#define IVC(ir) ivc_get(cache, mem, (ir) - lo, per, knots, n, k, q, x, (ir))
+        for (int64_t dc = 0; dc < W; ++dc) {
+            const int64_t c = a + dc - (k - 1);
+            if (c < 1 || c > nb) continue;
+            for (int64_t dd = 0; dd < W; ++dd) {
+                const int64_t d = b + dd - (k - 1);
+                if (d < 1 || d > nb) continue;
+                double *v = o + ((size_t)dc * W + (size_t)dd) * K1;
+                int64_t l1, h1, l2, h2;
+                pair_ivs(a, c, k, n_iv, &l1, &h1);
+                pair_ivs(b, d, k, n_iv, &l2, &h2);
+                /* 4d part: n over the (a, c) entries, m over the (b, d) entries,
+                 * both by ascending interval (or_rk_map's loop order) */
+                for (int64_t kk = 0; kk < K1; ++kk) {
+                    double acc = 0.0;
+                    for (int64_t iv1 = l1; iv1 <= h1; ++iv1) {
+                        double rk1, rmk1;
+                        prim_off(IVC(iv1), k, q, w, a, c, kk, &rk1, &rmk1);
+                        for (int64_t iv2 = l2; iv2 <= h2; ++iv2) {
+                            if (iv1 == iv2) continue;
+                            double rk2, rmk2;
+                            prim_off(IVC(iv2), k, q, w, b, d, kk, &rk2, &rmk2);
+                            if (iv1 < iv2)
+                                acc = acc + rk1 * rmk2;
+                            else
+                                acc = acc + rk2 * rmk1;
+                        }
+                    }
+                    v[kk] = acc;
+                }
+                /* 6d part: entries (ir; ib=a, ibp=c, jb=b, jbp=d) add through
+                 * their direct key, entries (ir; ib=b, ibp=d, jb=a, jbp=c)
+                 * through their swapped key; in the 6d COO order (jbp, jb,
+                 * ibp, ib, ir) one group precedes the other, or both are the
+                 * same entries (a = b, c = d), each adding twice */
+                int64_t s_lo = l1 > l2 ? l1 : l2, s_hi = h1 < h2 ? h1 : h2;
+                int same = (a == b && c == d);
+                int direct_first = (d < c) || (d == c && (b < a || (b == a && (c < d || (c == d && a < b)))));
+                for (int g = 0; g < 2; ++g) {
+                    int direct = same ? 1 : (g == 0 ? direct_first : !direct_first);
+                    if (same && g == 1) break;
+                    for (int64_t ir = s_lo; ir <= s_hi; ++ir) {
+                        for (int64_t kk = 0; kk < K1; ++kk) {
+                            double dv = direct ? prim_diag(IVC(ir), k, q, w, a, c, b, d, kk)
+                                               : prim_diag(IVC(ir), k, q, w, b, d, a, c, kk);
+                            v[kk] = v[kk] + dv;
+                            if (same) v[kk] = v[kk] + dv;
+                        }
+                    }
+                }
+            }
+        }
+#undef IVC
+        for (int64_t v = 0; v < niv; ++v) free(mem[v]);
+        free(mem);
+        free(cache);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* Basis enumeration (orbital_tools.f90:46-72, 119-216)                       */
 /* ------------------------------------------------------------------------ */
 
@@ -548,8 +732,19 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
                         int64_t row_end, int64_t *H_ptr, int64_t *H_idx, double *H_data,
                         double *H_scale, int64_t *S_ptr, int64_t *S_idx, double *S_data,
                         int64_t *nnz_out) {
+    or_construct_block_tiles(cf, n_config, L, spin, k, n_b, max_k, full, R, NULL, H1p, n_l, S,
+                             row_begin, row_end, H_ptr, H_idx, H_data, H_scale, S_ptr, S_idx,
+                             S_data, nnz_out);
+}
+
+void or_construct_block_tiles(const or_config *cf, int64_t n_config, int64_t L, int64_t spin,
+                              int64_t k, int64_t n_b, int64_t max_k, int64_t full,
+                              const double *R, const int64_t *tile_of, const double *H1p,
+                              int64_t n_l, const double *S, int64_t row_begin, int64_t row_end,
+                              int64_t *H_ptr, int64_t *H_idx, double *H_data, double *H_scale,
+                              int64_t *S_ptr, int64_t *S_idx, double *S_data, int64_t *nnz_out) {
     (void)n_l;
-    int64_t K1 = max_k + 1;
+    int64_t K1 = max_k + 1, W = 2 * k - 1;
     ang_cache ac;
     ang_cache_init(&ac, lmax_of(cf, n_config), K1, L);
     const double complex *Hc = (const double complex *)H1p;
@@ -565,6 +760,21 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
     double exsign = (spin != 0) ? -1.0 : 1.0;
     for (int64_t i = row_begin; i < row_end; ++i) {
         int64_t na = cf[i].n1, nbb = cf[i].n2, la = cf[i].l1, lb = cf[i].l2;
+        /* this row's R^k tile (a, b) = (na, nbb): banded store or tile table */
+        const double *Rt = NULL;
+        if (tile_of) {
+            int64_t ti = tile_of[(na - 1) * n_b + (nbb - 1)];
+            if (ti < 0) {
+                free(ac.v);
+                nnz_out[0] = -1;
+                nnz_out[1] = -1;
+                return;
+            }
+            Rt = R + (size_t)ti * W * W * K1;
+        } else {
+            Rt = R + rk_key(n_b, k, K1, na, nbb, na - k + 1, nbb - k + 1);
+        }
+#define RKT(c, d) (Rt + ((size_t)((c) - na + k - 1) * W + (size_t)((d) - nbb + k - 1)) * K1)
         for (int64_t j = full ? 0 : i; j < n_config; ++j) {
             int64_t nc = cf[j].n1, nd = cf[j].n2, lc = cf[j].l1, ld = cf[j].l2;
             int support = llabs(na - nc) < k && llabs(nbb - nd) < k;
@@ -588,7 +798,7 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
                 /* c_mat_neq_tens (mat_els.f90:608-633) with r_12_tens (:552-571) */
                 double res = 0.0;
                 if (support) {
-                    const double *vals = R + rk_key(n_b, k, K1, na, nbb, nc, nd);
+                    const double *vals = RKT(nc, nd);
                     double r = 0.0;
                     for (int64_t kk = 0; kk <= max_k; ++kk) {
                         double ang = ang_get(&ac, kk, la, lb, lc, ld);
@@ -599,7 +809,7 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
                     res = res + r;
                 }
                 if (support_ex) {
-                    const double *vals = R + rk_key(n_b, k, K1, na, nbb, nd, nc);
+                    const double *vals = RKT(nd, nc);
                     double r = 0.0;
                     for (int64_t kk = 0; kk <= max_k; ++kk) {
                         double ang = ang_get(&ac, kk, la, lb, ld, lc);
@@ -650,6 +860,7 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
             H_ptr[i - row_begin + 1] = rowH;
             S_ptr[i - row_begin + 1] = rowS;
         }
+#undef RKT
     }
 #undef SM
 #undef HM

@@ -61,6 +61,17 @@ void or_rk_map(int64_t n_b, int64_t k, int64_t max_k, int64_t nnz4, const double
                const double *rmk, const int64_t *idx4, int64_t nnz6, const double *rdk,
                const int64_t *idx6, double *R);
 
+/* R^k of whole tiles (a, b) for bases too large for or_slater + or_rk_map:
+ * out[t][dc][dd][kk] = R^k[a, b, a+dc-(k-1), b+dd-(k-1)] for tile t = (ab[2t],
+ * ab[2t+1]) (1-based), W = 2k-1 values of dc and dd, zero where c or d falls
+ * outside 1..n_b.  The primitives a key needs are computed with or_slater's
+ * arithmetic (compute_Slater_off_diag / compute_Slater_diag,
+ * mat_els.f90:392-491), spline values cached per interval, and added in the
+ * order compute_R_K_map (sparse_array_tools.f90:452-493) adds them into that
+ * key, so each value equals or_rk_map's bit for bit.  OpenMP over tiles. */
+void or_rk_tiles(const double *knots, int64_t n_knots, int64_t k, int64_t k_GL, int64_t max_k,
+                 int64_t n_tiles, const int64_t *ab, double *out, int nthreads);
+
 /* Configuration list of one symmetry block (src/tools/orbital_tools.f90:119-216).
  * spin = 0 is the reference (singlet); spin = 1 gives the triplet list.
  * Returns the count; writes the list when out != NULL. */
@@ -85,6 +96,17 @@ void or_construct_block(const or_config *cf, int64_t n_config, int64_t L, int64_
                         int64_t row_end, int64_t *H_ptr, int64_t *H_idx, double *H_data,
                         double *H_scale, int64_t *S_ptr, int64_t *S_idx, double *S_data,
                         int64_t *nnz_out);
+
+/* or_construct_block with R given as tiles (or_rk_tiles layout): the R^k
+ * values of row (n_a, n_b) are read from tile tile_of[(n_a-1)*n_b_total +
+ * (n_b-1)] of R (each row reads only its own tile).  A row whose tile is
+ * missing (index < 0) stops the assembly with nnz_out[0] = -1. */
+void or_construct_block_tiles(const or_config *cf, int64_t n_config, int64_t L, int64_t spin,
+                              int64_t k, int64_t n_b, int64_t max_k, int64_t full,
+                              const double *R, const int64_t *tile_of, const double *H1p,
+                              int64_t n_l, const double *S, int64_t row_begin, int64_t row_end,
+                              int64_t *H_ptr, int64_t *H_idx, double *H_data, double *H_scale,
+                              int64_t *S_ptr, int64_t *S_idx, double *S_data, int64_t *nnz_out);
 
 /* One-body matrices (src/mat_els/mat_els.f90:47-118, 294-346): S and
  * H_l = -1/2 d2/dr2 + l(l+1)/(2r^2) - Z/r + CAP, complex n_b x n_b column-major. */

@@ -49,6 +49,9 @@ def lib():
         "or_count_nnz": (None, [p, i64, i64, i64, i64, i64, i64, p]),
         "or_construct_block": (None, [p, i64, i64, i64, i64, i64, i64, i64, p, p, i64, p, i64,
                                       i64, p, p, p, p, p, p, p, p]),
+        "or_construct_block_tiles": (None, [p, i64, i64, i64, i64, i64, i64, i64, p, p, p, i64,
+                                            p, i64, i64, p, p, p, p, p, p, p, p]),
+        "or_rk_tiles": (None, [p, i64, i64, i64, i64, i64, p, p, ctypes.c_int]),
         "or_setup_S": (None, [p, i64, i64, i64, p]),
         "or_setup_H1p": (None, [p, i64, i64, i64, i64, i64, i64, dbl, dbl, dbl, p]),
         "or_setup_radial_dip": (None, [p, i64, i64, i64, i64, p, p, p]),
@@ -144,10 +147,34 @@ def count_nnz(cf, L, k, max_k, full=True, spin=0):
     return int(nnz[0]), int(nnz[1])
 
 
-def construct_block(cf, L, k, n_b, max_k, R, H1p, S, full=True, spin=0, rows=None):
+def rk_tiles(knots, k, k_GL, max_k, tiles, nthreads=0):
+    """R^k of whole tiles (a, b) (1-based pairs, n x 2) straight from the
+    knots: array (n, W, W, max_k+1) laid out like rk_map's R[a-1, b-1], each
+    value equal to rk_map's bit for bit (same primitives, same summation
+    order), without the full O(N^2 k^4) primitives."""
+    t = np.ascontiguousarray(knots, dtype=np.float64)
+    ab = np.ascontiguousarray(np.asarray(tiles, dtype=np.int64).reshape(-1, 2))
+    W = 2 * k - 1
+    out = np.zeros((ab.shape[0], W, W, max_k + 1))
+    lib().or_rk_tiles(_p(t), t.size, k, k_GL, max_k, ab.shape[0], _p(ab), _p(out), int(nthreads))
+    return out
+
+
+def tile_table(n_b, tiles):
+    """tile_of[(a-1)*n_b + (b-1)] = index of tile (a, b) in a rk_tiles array, -1 elsewhere."""
+    ab = np.asarray(tiles, dtype=np.int64).reshape(-1, 2)
+    tab = np.full(n_b * n_b, -1, dtype=np.int64)
+    tab[(ab[:, 0] - 1) * n_b + (ab[:, 1] - 1)] = np.arange(ab.shape[0])
+    return tab
+
+
+def construct_block(cf, L, k, n_b, max_k, R, H1p, S, full=True, spin=0, rows=None,
+                    tile_of=None):
     """construct_block_tensor for rows [r0, r1) (default: all).  Returns (H, S)
     dicts with 1-based CSR arrays local to the row range; H['scale'] holds the
-    sum of magnitudes of the terms of each entry."""
+    sum of magnitudes of the terms of each entry.  R is the banded rk_map
+    store, or (with tile_of from tile_table) a rk_tiles array holding the tile
+    (n1, n2) of every row of the range."""
     cf = np.ascontiguousarray(cf)
     r0, r1 = (0, cf.size) if rows is None else rows
     R = np.ascontiguousarray(R, dtype=np.float64)
@@ -156,16 +183,25 @@ def construct_block(cf, L, k, n_b, max_k, R, H1p, S, full=True, spin=0, rows=Non
     n_l = H1p.shape[2] if H1p.ndim == 3 else 1
     L_ = lib()
     nnz = np.zeros(2, dtype=np.int64)
-    args = [_p(cf), cf.size, L, spin, k, n_b, max_k, int(bool(full)), _p(R), _p(H1p), n_l,
-            _p(S), r0, r1]
-    L_.or_construct_block(*args, None, None, None, None, None, None, None, _p(nnz))
+    if tile_of is not None:
+        tile_of = np.ascontiguousarray(tile_of, dtype=np.int64)
+        args = [_p(cf), cf.size, L, spin, k, n_b, max_k, int(bool(full)), _p(R), _p(tile_of),
+                _p(H1p), n_l, _p(S), r0, r1]
+        fn = L_.or_construct_block_tiles
+    else:
+        args = [_p(cf), cf.size, L, spin, k, n_b, max_k, int(bool(full)), _p(R), _p(H1p), n_l,
+                _p(S), r0, r1]
+        fn = L_.or_construct_block
+    fn(*args, None, None, None, None, None, None, None, _p(nnz))
+    if nnz[0] < 0:
+        raise ValueError("construct_block: a row's R^k tile is not in the tile table")
     nh, ns = int(nnz[0]), int(nnz[1])
     n = r1 - r0
     H = dict(index_ptr=np.zeros(n + 1, np.int64), indices=np.zeros(nh, np.int64),
              data=np.zeros(nh, np.complex128), scale=np.zeros(nh), nnz=nh)
     Sd = dict(index_ptr=np.zeros(n + 1, np.int64), indices=np.zeros(ns, np.int64),
               data=np.zeros(ns, np.complex128), nnz=ns)
-    L_.or_construct_block(*args, _p(H["index_ptr"]), _p(H["indices"]), _p(H["data"]),
+    fn(*args, _p(H["index_ptr"]), _p(H["indices"]), _p(H["data"]),
                           _p(H["scale"]), _p(Sd["index_ptr"]), _p(Sd["indices"]),
                           _p(Sd["data"]), _p(nnz))
     return H, Sd

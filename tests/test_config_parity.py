@@ -1,0 +1,225 @@
+"""Oracle parity at the benchmark sizes, in the default GPU suite.
+
+Three workloads, each against the FP64 CPU oracle (the C restatement of the
+reference), on both the FP64 and the mixed path, through the C ABI:
+
+- order 7, N=200, r_max=200, q=10, k=0..10, l_max=5, L=0..3, singlet and
+  triplet (the medium drop-in size): the oracle's full primitives and R^k map
+  (slater + rk_map, the reference's own loops); EVERY element of the R^k store
+  for every multipole, and 64 rows (8 places x 8 rows) of each of the 8
+  symmetry blocks, whole rows with every column.
+- order 8, N=400, r_max=400, q=10, k=0..12, l_max=6, L=0..2 (the precision
+  study size) and order 9, N=800, r_max=800, q=12, k=0..20, l_max=10,
+  L=0..5 (the large size): the oracle builds whole R^k tiles (a, b) straight
+  from the knots (rk_tiles: the reference's primitives and summation order,
+  equal bit for bit to rk_map where both run); the R^k store is compared on a
+  spread of tiles (near the origin, near the diagonal, far field, last
+  splines) and on every tile a sampled row reads, and sampled rows of every
+  block are assembled by the oracle from those tiles.
+
+Bars: CSR patterns bit-exact; R^k elements within 1e-12 relative (both
+stores); H entries within 1e-12 of their term scale for the FP64 path and
+1e-11 for the mixed path, and per entry (entries >= 1e-15 Eh, see
+parity_util) within 1e-12 (FP64) and 1e-9 (mixed); S entries per entry
+within 1e-12.  The one-body matrices of both sides are their own (GPU
+bs2e_one_body, oracle setup_H1p / setup_S).  With BS2E_REPORT_DIR set, every
+figure is written there as JSON.
+"""
+import functools
+import time
+
+import numpy as np
+import pytest
+
+from parity_util import FLOOR, band_keys, errors, merge, oracle_rows, report, row_starts
+
+pytestmark = pytest.mark.gpu
+
+CAP = dict(cap_order=2, cap_r0=10.0, cap_eta=1e-3)
+W2 = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, lmax=5, max_L=3, spins=(0, 1), Z=2)
+W3 = dict(k=8, n_b=400, r_max=400.0, q=10, max_k=12, lmax=6, max_L=2, spins=(0,), Z=2)
+W5 = dict(k=9, n_b=800, r_max=800.0, q=12, max_k=20, lmax=10, max_L=5, spins=(0,), Z=2)
+BARS = {"fp64": dict(term=1e-12, entry=1e-12), "mixed": dict(term=1e-11, entry=1e-9)}
+
+
+def _blocks(bs2e, O, w):
+    out = []
+    for spin in w["spins"]:
+        for (L, M, par) in bs2e.basis.symmetries(w["max_L"], True):
+            out.append((L, par, spin, O.count_configs(L, par, w["lmax"], w["n_b"], w["k"],
+                                                     spin=spin)))
+    return out
+
+
+def _handle(bs2e, w, name):
+    prec = bs2e.PREC_MIXED if name == "mixed" else bs2e.PREC_FP64
+    t = bs2e.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    h = bs2e.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec)
+    h.slater()
+    h.rk()
+    h.one_body(w["Z"], w["lmax"] + 1, CAP["cap_order"], CAP["cap_r0"], CAP["cap_eta"],
+               copy_out=False)
+    return h
+
+
+def _one_body(O, t, w):
+    H1p = O.setup_H1p(t, w["k"], w["q"], w["Z"], w["lmax"] + 1, **CAP)
+    S = O.setup_S(t, w["k"], w["q"])
+    return H1p, S
+
+
+def _compare_rows(h, O, w, blocks, R, H1p, S, places, per, tile_of=None):
+    """GPU rows vs oracle rows: pattern bit-exact, error statistics per block."""
+    jobs, where = [], []
+    for bi, (L, par, spin, cf) in enumerate(blocks):
+        starts, n = row_starts(cf.size, places, per)
+        for r0 in starts:
+            kw = dict(full=True, spin=spin, rows=(r0, r0 + n))
+            if tile_of is not None:
+                kw["tile_of"] = tile_of
+            jobs.append(((cf, L, w["k"], w["n_b"], w["max_k"], R, H1p, S), kw))
+            where.append((bi, r0, n))
+    refs = oracle_rows(O, jobs)
+    per_block = {}
+    for (bi, r0, n), (Hr, Sr) in zip(where, refs):
+        L, par, spin, cf = blocks[bi]
+        Hg, Sg = h.block_rows(cf, L, r0, n, True, spin)
+        np.testing.assert_array_equal(Hg["index_ptr"], Hr["index_ptr"])
+        np.testing.assert_array_equal(Hg["indices"], Hr["indices"])
+        np.testing.assert_array_equal(Sg["index_ptr"], Sr["index_ptr"])
+        np.testing.assert_array_equal(Sg["indices"], Sr["indices"])
+        e = per_block.setdefault(bi, {"L": L, "spin": spin, "rows": int(cf.size), "H": [], "S": []})
+        e["H"].append(errors(Hg["data"], Hr["data"], Hr["scale"]))
+        e["S"].append(errors(Sg["data"], Sr["data"]))
+    out = []
+    for bi in sorted(per_block):
+        e = per_block[bi]
+        out.append({"L": e["L"], "spin": e["spin"], "rows": e["rows"],
+                    "sampled_rows": places * per, "H": merge(e["H"]), "S": merge(e["S"])})
+    return out
+
+
+def _check_rows(rep, name):
+    bar = BARS[name]
+    for b in rep:
+        H, S = b["H"], b["S"]
+        where = "L=%d spin=%d" % (b["L"], b["spin"])
+        # every entry: term scale; entries at or above the floor: per entry.
+        # Entries below the floor are mostly cancellations (terms of 1e-5 Eh
+        # summing to below 1e-15 Eh), where any FP64 summation order differs
+        # by ~1e-16 of the terms: the term-scale bar is their bar.
+        assert H["term_max"] <= bar["term"], (where, H)
+        assert H["entry_max"] <= bar["entry"], (where, H)
+        assert S["entry_max"] <= 1e-12, (where, S)
+
+
+# --------------------------------------------------------------------------
+# order 7, N=200: full oracle primitives and R^k map
+# --------------------------------------------------------------------------
+@functools.lru_cache(maxsize=1)
+def _oracle_order7(bs2e_mod_id):
+    import oracle as O
+    from conftest import load_package
+    bs2e = load_package()
+    w = W2
+    t = bs2e.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    t0 = time.perf_counter()
+    prim = O.slater(t, w["k"], w["q"], w["max_k"])
+    R = O.rk_map(w["n_b"], w["k"], w["max_k"], prim)
+    t_rad = time.perf_counter() - t0
+    H1p, S = _one_body(O, t, w)
+    return dict(R=R, H1p=H1p, S=S, blocks=_blocks(bs2e, O, w), oracle_radial_s=t_rad)
+
+
+@pytest.mark.parametrize("name", ["fp64", "mixed"])
+def test_order7_n200_rk_store_every_element(bs2e, oracle, name):
+    ref = _oracle_order7(id(bs2e))
+    w = W2
+    R = ref["R"]
+    with _handle(bs2e, w, name) as h:
+        per_k = []
+        for kk in range(w["max_k"] + 1):
+            r = R[..., kk]
+            mask = r != 0.0
+            g = h.rk_export(kk)
+            # zero exactly where the oracle's banded map is zero (outside the basis)
+            np.testing.assert_array_equal(g[~mask], 0.0)
+            rel = np.abs(g[mask] - r[mask]) / r[mask]
+            per_k.append({"k": kk, "elements": int(mask.sum()), "max": float(rel.max()),
+                          "rms": float(np.sqrt(np.mean(rel ** 2)))})
+    report("order7_n200_rk_store_" + name, {"per_k": per_k,
+                                            "oracle_radial_s": ref["oracle_radial_s"]})
+    assert max(p["max"] for p in per_k) <= 1e-12, per_k
+
+
+@pytest.mark.parametrize("name", ["fp64", "mixed"])
+def test_order7_n200_rows_every_block(bs2e, oracle, name):
+    ref = _oracle_order7(id(bs2e))
+    w = W2
+    with _handle(bs2e, w, name) as h:
+        rep = _compare_rows(h, oracle, w, ref["blocks"], ref["R"], ref["H1p"], ref["S"],
+                            places=8, per=8)
+    report("order7_n200_rows_" + name, rep)
+    assert len(rep) == 8
+    _check_rows(rep, name)
+
+
+# --------------------------------------------------------------------------
+# order 8, N=400 and order 9, N=800: oracle tiles
+# --------------------------------------------------------------------------
+def _sample_tiles(N, k):
+    pick = sorted({1, 2, k, N // 3, N // 2, N - k, N - 1, N})
+    tiles = {(a, b) for a in pick for b in pick}
+    m = N // 2
+    tiles |= {(m, m + d) for d in range(-(k - 1), k)}
+    return tiles
+
+
+def _tiles_case(bs2e, O, w, places, per):
+    t = bs2e.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    blocks = _blocks(bs2e, O, w)
+    tiles = _sample_tiles(w["n_b"], w["k"])
+    for (L, par, spin, cf) in blocks:
+        starts, n = row_starts(cf.size, places, per)
+        for r0 in starts:
+            tiles |= set(zip(cf["n1"][r0:r0 + n].tolist(), cf["n2"][r0:r0 + n].tolist()))
+    tiles = np.array(sorted(tiles), dtype=np.int64)
+    t0 = time.perf_counter()
+    T = O.rk_tiles(t, w["k"], w["q"], w["max_k"], tiles)
+    t_tiles = time.perf_counter() - t0
+    H1p, S = _one_body(O, t, w)
+    return dict(t=t, blocks=blocks, tiles=tiles, T=T, tile_of=O.tile_table(w["n_b"], tiles),
+                H1p=H1p, S=S, oracle_tiles_s=t_tiles)
+
+
+def _tiles_test(bs2e, O, w, ref, label, places, per):
+    keys, pos = band_keys(ref["tiles"], w["k"], w["n_b"])
+    want = ref["T"][pos[:, 0], pos[:, 1], pos[:, 2], :]
+    assert (want > 0).all()
+    out = {"tiles": int(len(ref["tiles"])), "keys": int(len(keys)),
+           "oracle_tiles_s": ref["oracle_tiles_s"]}
+    for name in ("fp64", "mixed"):
+        with _handle(bs2e, w, name) as h:
+            got = h.rk_get(keys)
+            rel = np.abs(got - want) / want
+            out["rk_" + name] = {"max": float(rel.max()), "rms": float(np.sqrt(np.mean(rel ** 2))),
+                                 "max_per_k": rel.max(axis=0).tolist()}
+            out["rows_" + name] = _compare_rows(h, O, w, ref["blocks"], ref["T"], ref["H1p"],
+                                                ref["S"], places, per, tile_of=ref["tile_of"])
+    report(label, out)
+    for name in ("fp64", "mixed"):
+        assert out["rk_" + name]["max"] <= 1e-12, (name, out["rk_" + name])
+        _check_rows(out["rows_" + name], name)
+    return out
+
+
+def test_order8_n400_tiles_and_rows(bs2e, oracle):
+    w = W3
+    ref = _tiles_case(bs2e, oracle, w, places=8, per=8)
+    _tiles_test(bs2e, oracle, w, ref, "order8_n400_parity", 8, 8)
+
+
+def test_order9_n800_tiles_and_rows(bs2e, oracle):
+    w = W5
+    ref = _tiles_case(bs2e, oracle, w, places=6, per=8)
+    _tiles_test(bs2e, oracle, w, ref, "order9_n800_parity", 6, 8)

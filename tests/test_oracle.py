@@ -146,3 +146,32 @@ def test_block_symmetric_without_cap(oracle, bs2e):
         A = {(i, j): v for i, j, v in zip(rows, cols, H["data"])}
         for (i, j), v in list(A.items())[::97]:
             assert abs(A[(j, i)] - v) <= 1e-12 * max(1.0, abs(v))
+
+
+@pytest.mark.parametrize("case", ["ref60", "small2", "bigtile"])
+def test_rk_tiles_equal_full_map(oracle, bs2e, case):
+    """rk_tiles (whole R^k tiles straight from the knots, used where the full
+    primitives are too slow) equals the full slater + rk_map store bit for
+    bit on every tile, and the tile-table construct equals the banded one."""
+    c = CASES[case]
+    ref = oracle_reference(case)
+    N, k = c["n_b"], c["k"]
+    tiles = np.array([(a, b) for a in range(1, N + 1) for b in range(1, N + 1)])
+    T = oracle.rk_tiles(ref["knots"], k, c["q"], c["max_k"], tiles)
+    np.testing.assert_array_equal(T, ref["R"].reshape(N * N, *ref["R"].shape[2:]))
+    for (L, M, par, spin, cf) in blocks(bs2e, case)[:2]:
+        r0, r1 = 1, min(cf.size, 30)
+        need = np.unique(np.stack([cf["n1"][r0:r1], cf["n2"][r0:r1]], 1), axis=0)
+        Tn = oracle.rk_tiles(ref["knots"], k, c["q"], c["max_k"], need)
+        args = (cf, L, k, N, c["max_k"])
+        Ha, Sa = oracle.construct_block(*args, ref["R"], ref["H1p"], ref["S"], True, spin,
+                                        rows=(r0, r1))
+        Hb, Sb = oracle.construct_block(*args, Tn, ref["H1p"], ref["S"], True, spin,
+                                        rows=(r0, r1), tile_of=oracle.tile_table(N, need))
+        for x in ("index_ptr", "indices", "data", "scale"):
+            np.testing.assert_array_equal(Ha[x], Hb[x])
+        for x in ("index_ptr", "indices", "data"):
+            np.testing.assert_array_equal(Sa[x], Sb[x])
+    with pytest.raises(ValueError):
+        oracle.construct_block(*args, Tn[:1], ref["H1p"], ref["S"], True, spin, rows=(r0, r1),
+                               tile_of=oracle.tile_table(N, need[:1]))
