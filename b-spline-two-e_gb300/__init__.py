@@ -99,6 +99,9 @@ def lib():
         "bs2e_block_band_count": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p]),
         "bs2e_block_fill_band": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, p]),
         "bs2e_set_block_cache": (st, [p, i64]),
+        "bs2e_band_plan": (st, [i64, p, p, i64, i64, i64, p, p]),
+        "bs2e_band_rows": (st, [p, i64, i64, i64, p, p]),
+        "bs2e_band_merge": (st, [i64, i64, p, p, p, p, p, p, p, p]),
         "bs2e_set_one_body": (st, [p, p, i64, p]),
         "bs2e_one_body": (st, [p, i64, i64, i64, dbl, dbl, dbl, p, p]),
         "bs2e_block_count": (st, [p, p, i64, i64, i64, p, p]),
@@ -206,6 +209,59 @@ def write_block(path, blocks, n_rows_b, n_cols_b, max_subrecord=0):
     shapes, nnz, P, I, D, keep = _block_arrays(order)
     _check(None, lib().bs2e_write_block(os.fsencode(path), n_rows_b, n_cols_b, _ptr(shapes),
                                         _ptr(nnz), P, I, D, int(max_subrecord)))
+
+
+def band_plan(per_n1, max_bytes, n_ranks=1):
+    """Bands of every block that fit max_bytes, each with its owner rank
+    (bs2e_band_plan): per_n1[b] is block b's (n1_max, 3) array of (rows,
+    nnz_H, nnz_S) per n1.  Returns an (n_bands, 5) array of (block, n1_first,
+    n1_count, owner, bytes)."""
+    per = [np.ascontiguousarray(p, dtype=np.int64) for p in per_n1]
+    nmax = np.array([p.shape[0] for p in per], dtype=np.int64)
+    ptrs = (ctypes.c_void_p * max(len(per), 1))(*[p.ctypes.data for p in per])
+    n = ctypes.c_int64()
+    st = lib().bs2e_band_plan(len(per), _ptr(nmax), ptrs, int(max_bytes), int(n_ranks), 0, None,
+                              ctypes.byref(n))
+    if st != 0 and n.value == 0:
+        _check(None, st)
+    out = np.zeros((max(n.value, 1), 5), dtype=np.int64)
+    _check(None, lib().bs2e_band_plan(len(per), _ptr(nmax), ptrs, int(max_bytes), int(n_ranks),
+                                      n.value, _ptr(out), ctypes.byref(n)))
+    return out[:n.value]
+
+
+def band_rows(cf, n1_first, n1_count):
+    """1-based block rows of an n1 band (bs2e_band_rows)."""
+    cf = as_configs(cf)
+    n = ctypes.c_int64()
+    _check(None, lib().bs2e_band_rows(_ptr(cf), cf.size, int(n1_first), int(n1_count), None,
+                                      ctypes.byref(n)))
+    rows = np.zeros(max(n.value, 1), dtype=np.int64)
+    _check(None, lib().bs2e_band_rows(_ptr(cf), cf.size, int(n1_first), int(n1_count),
+                                      _ptr(rows), ctypes.byref(n)))
+    return rows[:n.value]
+
+
+def band_merge(n_config, bands):
+    """Joins band CSRs into the block CSR (bs2e_band_merge): bands is a list
+    of dicts with 'rows' (1-based block rows), 'index_ptr', 'indices', 'data'."""
+    nb = len(bands)
+    arr = lambda xs, t: (ctypes.c_void_p * max(nb, 1))(*[x.ctypes.data for x in xs])
+    rows = [np.ascontiguousarray(b["rows"], dtype=np.int64) for b in bands]
+    ptr = [np.ascontiguousarray(b["index_ptr"], dtype=np.int64) for b in bands]
+    idx = [np.ascontiguousarray(b["indices"], dtype=np.int64) for b in bands]
+    dat = [np.ascontiguousarray(b["data"], dtype=np.complex128) for b in bands]
+    nrows = np.array([r.size for r in rows], dtype=np.int64)
+    nnz = int(sum(int(p[-1]) - 1 for p in ptr))
+    out = dict(index_ptr=np.zeros(n_config + 1, np.int64), indices=np.zeros(max(nnz, 1), np.int64),
+               data=np.zeros(max(nnz, 1), np.complex128))
+    _check(None, lib().bs2e_band_merge(int(n_config), nb, _ptr(nrows), arr(rows, 0), arr(ptr, 0),
+                                       arr(idx, 0), arr(dat, 0), _ptr(out["index_ptr"]),
+                                       _ptr(out["indices"]), _ptr(out["data"])))
+    out["indices"] = out["indices"][:nnz]
+    out["data"] = out["data"][:nnz]
+    out["nnz"] = nnz
+    return out
 
 
 def _check(h, status):

@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libbs2e.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 SOURCES = ["bs2e_capi.cu", "bs2e_radial.cu", "bs2e_assembly.cu", "bs2e_dipole.cu",
            "bs2e_noalloc.cu", "bs2e_angular.cpp", "bs2e_basis.cpp", "bs2e_fortio.cpp",
-           "bs2e_spmv.cu", "bs2e_batch.cu", "bs2e_blockcsr.cu"]
+           "bs2e_spmv.cu", "bs2e_batch.cu", "bs2e_blockcsr.cu", "bs2e_bands.cpp"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(HERE, "..", "include")]
 
@@ -65,6 +65,26 @@ def build(force=False):
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "..", "tests", "capi_driver.c")
+DRIVER = os.path.join(HERE, "..", "tests", "_build", "capi_driver")
+
+
+def build_driver():
+    """Compiles the plain-C caller of include/bs2e.h (tests/capi_driver.c)
+    with the host C compiler, strict C11 with warnings as errors, linked
+    against libbs2e.so: the header's declarations meet a C compiler and every
+    entry point it calls must resolve in the library."""
+    os.makedirs(os.path.dirname(DRIVER), exist_ok=True)
+    cc = os.environ.get("CC", "gcc")
+    cmd = [cc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic", "-O1",
+           "-I" + os.path.join(HERE, "..", "include"), DRIVER_SRC, "-L" + HERE, "-lbs2e",
+           "-Wl,-rpath," + HERE, "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("C driver build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    return DRIVER
 
 
 def build_oracle():

@@ -293,6 +293,7 @@ struct FillArgs {
     const int64_t *Hptr, *Sptr;
     int64_t row0, row1, ptr_row0, Hbase, Sbase;
     const int *band;
+    int64_t band_rows;  // rows of the band (pointer slots 0..band_rows)
     int a0;  // tile (n_a, n_b) of CTA x: n_a = a0 + x / N, n_b = x % N + 1
     int64_t *Hidx, *Sidx;
     double2 *Hdat, *Sdat;
@@ -1030,9 +1031,19 @@ __global__ void __launch_bounds__(128, MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_
         int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
         const int64_t row = base + (n_b - lo);
         if (base >= 0 && lo <= n_b && n_b <= hi && row >= F.row0 && row < F.row1) {
+            int local = (int)(row - F.ptr_row0);
+            if (F.band) {
+                // a row outside the band's list would write past its pointer
+                // arrays: skip it and report (error word 2)
+                const int64_t loc = (int64_t)F.band[A.n_ch + c] + (row - F.band[c]);
+                if (row < F.band[c] || loc >= F.band_rows) {
+                    atomicExch(F.err, 2);
+                    continue;
+                }
+                local = (int)loc;
+            }
             int slot = atomicAdd(&snrow, 1);
-            srow[slot] = F.band ? F.band[A.n_ch + c] + (int)(row - F.band[c])
-                                : (int)(row - F.ptr_row0);
+            srow[slot] = local;
             sch[slot] = c;
         }
     }
@@ -1241,6 +1252,7 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     F.Sbase = r.Sbase;
     F.a0 = r.a0;
     F.band = r.band;
+    F.band_rows = r.band_rows;
     size_t smem = fill_smem(h->g);
     if (h->plan.n_config > 0 && r.row1 > r.row0 && r.rows_mode) {
         const unsigned grid = (unsigned)((r.row1 - r.row0 + 3) / 4);

@@ -64,6 +64,9 @@ bs2e_status sync_check(bs2e_handle *h, const char *what) {
     CU(cudaMemcpy(&e, h->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) {
         cudaMemset(h->d_err, 0, sizeof(int));
+        if (e == 2)
+            return fail(h, BS2E_ERR_COUNT,
+                        std::string(what) + ": a row outside the band's row list was skipped");
         return fail(h, BS2E_ERR_TIMEOUT, std::string(what) + ": a bounded device wait expired");
     }
     return BS2E_OK;
@@ -1246,14 +1249,16 @@ static bs2e_status ensure_prefix(bs2e_handle *h) {
     return BS2E_OK;
 }
 
-// Band boundaries of the counted block: rows[c * (nx + 1) + j] is the first
-// row of channel c with n1 >= x0 + j (j = 0..nx; channel c holds rows
-// [ch_start[c], ch_start[c + 1])), PH / PS the block's 1-based pointers there.
-static bs2e_status band_bounds(bs2e_handle *h, const bs2e_config *cf, int64_t x0, int64_t nx,
-                               std::vector<int64_t> &rows, std::vector<int64_t> &PH,
-                               std::vector<int64_t> &PS) {
+// Band boundaries of the counted block: for the ascending n1 values xs[0..nx],
+// rows[c * (nx + 1) + j] is the first row of channel c with n1 >= xs[j]
+// (channel c holds rows [ch_start[c], ch_start[c + 1])), PH / PS the block's
+// 1-based pointers there.
+static bs2e_status band_bounds(bs2e_handle *h, const bs2e_config *cf,
+                               const std::vector<int64_t> &xs, std::vector<int64_t> &rows,
+                               std::vector<int64_t> &PH, std::vector<int64_t> &PS) {
     const BlockPlan &P = h->plan;
     const int n_ch = P.n_ch;
+    const int64_t nx = (int64_t)xs.size() - 1;
     const int64_t m = (int64_t)n_ch * (nx + 1);
     rows.assign((size_t)m, 0);
     for (int c = 0; c < n_ch; ++c) {
@@ -1264,7 +1269,7 @@ static bs2e_status band_bounds(bs2e_handle *h, const bs2e_config *cf, int64_t x0
             int64_t a = r, b = hi;
             while (a < b) {
                 const int64_t mid = a + (b - a) / 2;
-                if (cf[mid].n1 < x0 + j) a = mid + 1;
+                if (cf[mid].n1 < xs[(size_t)j]) a = mid + 1;
                 else b = mid;
             }
             r = a;
@@ -1302,11 +1307,17 @@ BS2E_API bs2e_status bs2e_block_band_count(bs2e_handle *h, const bs2e_config *co
                                            int64_t *per_n1) {
     if (!h || n_config < 0 || !n_rows || !nnz_H || !nnz_S || n1_count < 0) return BS2E_ERR_ARG;
     Guard G(h);
-    if (n1_count > (int64_t)1 << 24) return fail(h, BS2E_ERR_ARG, "n1_count too large");
+    if (n1_count > (int64_t)1 << 24 || n1_first < -((int64_t)1 << 40) ||
+        n1_first > ((int64_t)1 << 40))
+        return fail(h, BS2E_ERR_ARG, "n1 range out of bounds");
     TRY(ensure_counted(h, configs, n_config, L, spin, full));
-    std::vector<int64_t> rows, PH, PS;
+    std::vector<int64_t> rows, PH, PS, xs;
     const int64_t nx = per_n1 ? n1_count : 1;
-    TRY(band_bounds(h, configs, n1_first, nx, rows, PH, PS));
+    if (per_n1)
+        for (int64_t j = 0; j <= n1_count; ++j) xs.push_back(n1_first + j);
+    else
+        xs = {n1_first, n1_first + n1_count};
+    TRY(band_bounds(h, configs, xs, rows, PH, PS));
     const int n_ch = h->plan.n_ch;
     int64_t r = 0, eh = 0, es = 0;
     if (per_n1) memset(per_n1, 0, sizeof(int64_t) * 3 * (size_t)n1_count);
@@ -1337,9 +1348,12 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
                                           double *S_data) {
     if (!h || n_config < 0 || n1_count < 0) return BS2E_ERR_ARG;
     Guard G(h);
+    if (n1_count > ((int64_t)1 << 40) || n1_first < -((int64_t)1 << 40) ||
+        n1_first > ((int64_t)1 << 40))
+        return fail(h, BS2E_ERR_ARG, "n1 range out of bounds");
     TRY(fill_ready(h, configs, n_config, L, spin, full));
     std::vector<int64_t> rows, PH, PS;
-    TRY(band_bounds(h, configs, n1_first, 1, rows, PH, PS));
+    TRY(band_bounds(h, configs, {n1_first, n1_first + n1_count}, rows, PH, PS));
     const int n_ch = h->plan.n_ch;
     std::vector<int> band(2 * (size_t)std::max(n_ch, 1), 0);
     std::vector<int64_t> boff(2 * ((size_t)n_ch + 1), 0);
@@ -1379,6 +1393,7 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
         r.a0 = (int)a0;
         r.a1 = (int)a1;
         r.band = h->d_band;
+        r.band_rows = nr;
         launch_block_fill(h, r, H_index_ptr, S_index_ptr, H_indices, (double2 *)H_data,
                           S_indices, (double2 *)S_data);
     }

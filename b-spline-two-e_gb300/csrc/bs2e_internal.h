@@ -280,6 +280,7 @@ struct FillRange {
     int a0 = 1, a1 = 0;
     bool rows_mode = false;
     const int *band = nullptr;
+    int64_t band_rows = 0;  // rows of the band when band is set
 };
 // out[i] = src[idx[i]] for i < n (device arrays)
 void launch_gather_i64(bs2e_handle *h, const int64_t *src, const int64_t *idx, int64_t n,

@@ -343,6 +343,46 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
                                           int64_t *S_index_ptr, int64_t *S_indices,
                                           double *S_data);
 
+/* Host-side planning of band work (no device, no handle; safe to call from
+ * any thread or rank).  Multi-GPU assembly hands each rank whole bands: the
+ * blocks are independent and a band's rows are independent of every other
+ * band's (no exchange step), so ranks fill disjoint bands and the rank that
+ * needs whole blocks gathers them (bs2e_band_merge), as CS_from_block_diag
+ * joins blocks (src/tools/block_tools.f90:289-348).
+ *
+ * bs2e_band_plan cuts every block into n1 bands whose CSR (24 bytes per
+ * non-zero of H and S plus 16 bytes per row) fits max_bytes, from per-n1
+ * counts (bs2e_block_band_count with per_n1): block b has n1 = 1..n1_max[b]
+ * and per_n1[b] holds (rows, nnz_H, nnz_S) per n1.  Bands are then assigned
+ * to n_ranks ranks, largest first to the least loaded rank (ties to the
+ * lower rank), so every rank computes the same plan without communicating.
+ * Band i is bands[5*i .. 5*i+4] = (block, n1_first, n1_count, owner rank,
+ * bytes), blocks in order, n1 ascending; *n_bands is set even when cap is too
+ * small (BS2E_ERR_ARG, nothing written).  A single n1 above max_bytes is an
+ * error (BS2E_ERR_ARG). */
+BS2E_API bs2e_status bs2e_band_plan(int64_t n_blocks, const int64_t *n1_max,
+                                    const int64_t *const *per_n1, int64_t max_bytes,
+                                    int64_t n_ranks, int64_t cap, int64_t *bands,
+                                    int64_t *n_bands);
+/* The 1-based block rows of band [n1_first, n1_first + n1_count) of a
+ * configuration list in basis order (the rows bs2e_block_fill_band writes, in
+ * the same order); rows may be NULL to count only. */
+BS2E_API bs2e_status bs2e_band_rows(const bs2e_config *configs, int64_t n_config,
+                                    int64_t n1_first, int64_t n1_count, int64_t *rows,
+                                    int64_t *n_rows);
+/* Joins bands of one block into the block's CSR (host arrays): band i has
+ * n_rows[i] rows with 1-based block rows rows[i], range-local 1-based
+ * index_ptr[i] (n_rows[i] + 1), indices[i] and complex128 data[i].  The
+ * bands' rows must cover 1..n_config exactly once (BS2E_ERR_ARG otherwise);
+ * out_index_ptr (n_config + 1), out_indices and out_data are sized by the
+ * sum of the bands' non-zeros. */
+BS2E_API bs2e_status bs2e_band_merge(int64_t n_config, int64_t n_bands, const int64_t *n_rows,
+                                     const int64_t *const *rows,
+                                     const int64_t *const *index_ptr,
+                                     const int64_t *const *indices, const double *const *data,
+                                     int64_t *out_index_ptr, int64_t *out_indices,
+                                     double *out_data);
+
 /* How many counted blocks the handle keeps besides the current one (0..16;
  * 16 at creation).  A kept block is reused when the same configuration list
  * is counted or filled again, skipping its planning and count pass; with 0
