@@ -97,7 +97,8 @@ def lib():
         "bs2e_block_count_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p]),
         "bs2e_block_fill_rows": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, i64]),
         "bs2e_block_band_count": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p]),
-        "bs2e_block_fill_band": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, p]),
+        "bs2e_block_fill_band": (st, [p, p, i64, i64, i64, i64, i64, i64, p, p, p, p, p, p, p,
+                                      i64]),
         "bs2e_set_block_cache": (st, [p, i64]),
         "bs2e_band_plan": (st, [i64, p, p, i64, i64, i64, p, p]),
         "bs2e_band_rows": (st, [p, i64, i64, i64, p, p]),
@@ -447,7 +448,29 @@ class Bs2e:
         rp = ctypes.c_void_p(int(rows)) if rows else None
         _check(self._h, lib().bs2e_block_fill_band(self._h, _ptr(cf), cf.size, int(L), int(spin),
                                                    int(bool(full)), int(n1_first), int(n1_count),
-                                                   rp, *args))
+                                                   rp, *args, 1))
+
+    def band_host_into(self, cf, L, n1_first, n1_count, full, spin, H, S, rows=None):
+        """Band fill into host numpy arrays (dicts 'index_ptr', 'indices',
+        'data'; rows: int64 array or None), staged through HBM."""
+        cf = as_configs(cf)
+        args = [_ptr(H[x]) for x in ("index_ptr", "indices", "data")]
+        args += [_ptr(S[x]) for x in ("index_ptr", "indices", "data")]
+        _check(self._h, lib().bs2e_block_fill_band(self._h, _ptr(cf), cf.size, int(L), int(spin),
+                                                   int(bool(full)), int(n1_first), int(n1_count),
+                                                   _ptr(rows), *args, 0))
+
+    def band(self, cf, L, n1_first, n1_count, full=True, spin=0):
+        """(rows, H, S) of an n1 band in host arrays."""
+        r, nh, ns = self.band_count(cf, L, n1_first, n1_count, full, spin)
+        mk = lambda n, m: dict(index_ptr=np.zeros(n + 1, np.int64),
+                               indices=np.zeros(max(m, 1), np.int64),
+                               data=np.zeros(max(m, 1), np.complex128), nnz=m)
+        H, S, rows = mk(r, nh), mk(r, ns), np.zeros(max(r, 1), np.int64)
+        self.band_host_into(cf, L, n1_first, n1_count, full, spin, H, S, rows)
+        for M, m in ((H, nh), (S, ns)):
+            M["indices"], M["data"] = M["indices"][:m], M["data"][:m]
+        return rows[:r], H, S
 
     def set_block_cache(self, n_blocks):
         """Counted blocks kept besides the current one (0..16)."""
@@ -539,6 +562,15 @@ class Bs2e:
                                                    *[int(x) for x in sym2], int(q),
                                                    int(bool(compute)), ctypes.byref(n)))
         return n.value
+
+    def dip_block_into(self, rows, sym1, cols, sym2, q, D, compute=True):
+        """Dipole block fill into device buffers: D holds integer device
+        addresses under 'index_ptr', 'indices', 'data' (sized by dip_block_count)."""
+        rows, cols = as_configs(rows), as_configs(cols)
+        _check(self._h, lib().bs2e_dip_block_fill(
+            self._h, _ptr(rows), rows.size, *[int(x) for x in sym1], _ptr(cols), cols.size,
+            *[int(x) for x in sym2], int(q), int(bool(compute)),
+            *[ctypes.c_void_p(int(D[x])) for x in ("index_ptr", "indices", "data")], 1))
 
     def dip_block(self, rows, sym1, cols, sym2, q, compute=True):
         """Dipole block between symmetries sym1 = (L1, M1, parity1) (rows) and

@@ -1229,6 +1229,21 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
     return sync_check(h, "block fill (rows)");
 }
 
+// The two HBM staging areas of host-output fills, each at least `bytes`.
+static bs2e_status ensure_stage(bs2e_handle *h, int64_t bytes) {
+    if (bytes <= h->stage_cap && h->d_stage[0] && h->d_stage[1]) return BS2E_OK;
+    if (h->copy_stream) CU(cudaStreamSynchronize(h->copy_stream));
+    CU(cudaStreamSynchronize(h->stream));
+    dfree(h->d_stage[0]);
+    dfree(h->d_stage[1]);
+    h->stage_cap = 0;
+    const int64_t want = std::max<int64_t>(bytes, 256);
+    CU(dalloc(&h->d_stage[0], (size_t)want));
+    CU(dalloc(&h->d_stage[1], (size_t)want));
+    h->stage_cap = want;
+    return BS2E_OK;
+}
+
 // 1-based CSR pointers of the whole counted block (a scan of its row
 // counts), built once per counted block for band fills.
 static bs2e_status ensure_prefix(bs2e_handle *h) {
@@ -1345,7 +1360,7 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
                                           int64_t *rows_out, int64_t *H_index_ptr,
                                           int64_t *H_indices, double *H_data,
                                           int64_t *S_index_ptr, int64_t *S_indices,
-                                          double *S_data) {
+                                          double *S_data, int64_t out_on_device) {
     if (!h || n_config < 0 || n1_count < 0) return BS2E_ERR_ARG;
     Guard G(h);
     if (n1_count > ((int64_t)1 << 40) || n1_first < -((int64_t)1 << 40) ||
@@ -1369,10 +1384,42 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
     if (!H_index_ptr || !S_index_ptr || (nH > 0 && (!H_indices || !H_data)) ||
         (nS > 0 && (!S_indices || !S_data)))
         return fail(h, BS2E_ERR_ARG, "NULL output array");
-    if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
-        !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16) ||
-        !aligned(rows_out, 8))
-        return fail(h, BS2E_ERR_ARG, "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
+    // device arrays the kernels write: the caller's, or places in a staging area
+    const bool dev = out_on_device != 0;
+    int64_t *dHp = H_index_ptr, *dSp = S_index_ptr, *dRows = rows_out, *dHi = H_indices,
+            *dSi = S_indices;
+    double2 *dHd = (double2 *)H_data, *dSd = (double2 *)S_data;
+    if (dev) {
+        if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
+            !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16) ||
+            !aligned(rows_out, 8))
+            return fail(h, BS2E_ERR_ARG,
+                        "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
+    } else {
+        int64_t off = 0;
+        auto take = [&](int64_t bytes) {
+            const int64_t o = off;
+            off += (bytes + 255) / 256 * 256;
+            return o;
+        };
+        const int64_t oHp = take(8 * (nr + 1)), oSp = take(8 * (nr + 1)),
+                      oR = take(rows_out ? 8 * nr : 0), oHi = take(8 * nH), oSi = take(8 * nS),
+                      oHd = take(16 * nH), oSd = take(16 * nS);
+        if (off > h->stage_limit)
+            return fail(h, BS2E_ERR_ARG, "band fill into host arrays: the band needs " +
+                                             std::to_string(off) +
+                                             " bytes, more than a staging area; choose a "
+                                             "narrower band or raise bs2e_opts.stage_bytes");
+        TRY(ensure_stage(h, off));
+        unsigned char *b = h->d_stage[0];
+        dHp = (int64_t *)(b + oHp);
+        dSp = (int64_t *)(b + oSp);
+        dRows = rows_out ? (int64_t *)(b + oR) : nullptr;
+        dHi = (int64_t *)(b + oHi);
+        dSi = (int64_t *)(b + oSi);
+        dHd = (double2 *)(b + oHd);
+        dSd = (double2 *)(b + oSd);
+    }
     if (!h->d_band) CU(dalloc(&h->d_band, (size_t)2 * kMaxCh));
     if (!h->d_band_val) {
         CU(dalloc(&h->d_band_idx, (size_t)2 * (kMaxCh + 1)));
@@ -1383,7 +1430,7 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
                        h->stream));
     CU(cudaMemcpyAsync(h->d_band_val, boff.data(), sizeof(int64_t) * boff.size(),
                        cudaMemcpyHostToDevice, h->stream));
-    launch_band_ptr(h, h->d_band, h->d_band_val, n_ch, nr, H_index_ptr, S_index_ptr, rows_out);
+    launch_band_ptr(h, h->d_band, h->d_band_val, n_ch, nr, dHp, dSp, dRows);
     const int64_t a0 = std::max<int64_t>(n1_first, 1),
                   a1 = std::min<int64_t>(n1_first + n1_count - 1, h->g.N);
     if (nr > 0 && a1 >= a0) {
@@ -1394,10 +1441,23 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
         r.a1 = (int)a1;
         r.band = h->d_band;
         r.band_rows = nr;
-        launch_block_fill(h, r, H_index_ptr, S_index_ptr, H_indices, (double2 *)H_data,
-                          S_indices, (double2 *)S_data);
+        launch_block_fill(h, r, dHp, dSp, dHi, dHd, dSi, dSd);
     }
     CU(cudaGetLastError());
+    if (!dev) {
+        auto d2h = [&](void *dst, const void *src, int64_t bytes) {
+            return bytes > 0 ? cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost,
+                                               h->stream)
+                             : cudaSuccess;
+        };
+        CU(d2h(H_index_ptr, dHp, 8 * (nr + 1)));
+        CU(d2h(S_index_ptr, dSp, 8 * (nr + 1)));
+        if (rows_out) CU(d2h(rows_out, dRows, 8 * nr));
+        CU(d2h(H_indices, dHi, 8 * nH));
+        CU(d2h(S_indices, dSi, 8 * nS));
+        CU(d2h(H_data, dHd, 16 * nH));
+        CU(d2h(S_data, dSd, 16 * nS));
+    }
     return sync_check(h, "block fill (band)");
 }
 

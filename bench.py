@@ -1,42 +1,50 @@
 """Benchmark of the two-electron matrix-element path (R^k + 2e-H assembly).
 
-Workload (the "plain FP64 GPU drop-in at medium size" configuration): helium-like
-Z=2, B-spline order 7, N=200 on the exp-linear knot grid to r_max=200 a.u.,
-10 Gauss-Legendre points per interval, multipoles k=0..10, l_max=5, total
-L=0..3 (natural parity), singlet and triplet, full blocks.  One step is the
-whole path on the GPU: Slater primitives, the R^k store, the one-body matrices
-and count + fill of all 8 symmetry blocks.
+Default workload, the large form: helium-like Z=2, B-spline order 9, N=800 on
+the exp-linear knot grid to r_max=800 a.u., 12 Gauss-Legendre points per
+interval, multipoles k=0..20, l_max=10, singlet L=0..5 (natural parity), full
+blocks, with the L -> L+1 dipole blocks (q=0, length gauge).  One job is the
+whole path on the GPU: Slater primitives, the R^k store (3.84e9 elements,
+31 GB), one-body and radial dipole matrices, the count pass of every block,
+and the assembly of the 6 symmetry blocks (5.3e11 H and S entries) and the
+5 dipole blocks (~6e10 entries): ~14 TB of CSR, more than HBM and host memory
+together.  The CSR is therefore made in n1 bands (bs2e_block_fill_band) and
+dipole row slices of at most one staging area (24 GiB) and consumed on the
+device as it is made: the mat-vec bs2e_csr_mv applies every band of H and S
+and every slice of D to a fixed vector (the product a solver needs).
 
-value : R^k elements/s = P^2 (max_k+1) / step time, outputs written into
-        device buffers (inputs resident).  P = ordered band pairs = 2,558.
-e2e   : same metric through the C ABI with host output buffers (pinned): the
-        configuration lists go host->device and every CSR block device->host.
-roofline: the CSR fill kernel (k_csr_fill), timed with CUDA events on the
-        library's stream; algorithmic bytes = 24 B per stored H/S entry
-        (int64 index + complex128 value) + the R^k tiles it stages.  traffic:
-        DRAM bytes per launch, from the ncu capture of block 0 (profiles/
-        k_csr_fill_order7_n200_block0.md) scaled to the average launch by
-        algorithmic bytes.
-cpu_baseline: the CPU oracle (C restatement of the reference, OpenMP) on a
-        bounded sample: full Slater primitives + R^k map, and a row sample of
-        every block extrapolated to the full block (one thread per block, the
-        reference's OpenMP-over-symmetries decomposition).
+A bench step is 1/16 of a job: the job's bands and slices cut into 16
+chunks of nearly equal CSR bytes, chunk 0 also running the radial stage, so
+K steps process K/16 jobs and the timed region of K >= 16 steps holds at
+least one whole job, whose time is reported as job_s.
+
+value : R^k elements per job x jobs done / time (device-resident inputs and
+        outputs; jobs done counted by CSR bytes of the chunks run).
+e2e   : the same chunks through the C ABI with HOST buffers: configuration
+        lists from pinned host memory, every band and slice copied into
+        pinned host buffers (bs2e_block_fill_band / bs2e_dip_block_fill with
+        host outputs).
+mixed : the same job on the mixed-precision path (BS2E_PREC_MIXED), its time
+        and its error against the FP64 path on sampled bands.
+roofline: the band fill (k_csr_fill), timed with CUDA events on the
+        library's stream; algorithmic bytes = 24 B per stored H/S entry + the
+        band's 1-based pointers + the R^k tiles it stages; traffic = DRAM
+        bytes per algorithmic byte of an ncu capture of one band, scaled.
+cpu_baseline / --impl reference: the CPU oracle (the C restatement of the
+        reference, all host threads) on the same fraction f of every stage of
+        the job -- f of the R^k tiles, of every block's rows and of every
+        dipole block's rows -- so value = f x R^k elements / time.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                [--precision fp64|mixed] [--no-e2e] [--no-cpu-baseline]
-python bench.py --profile-block B   one radial pass and one count + fill of block B
-                                    (0 = L=0 singlet, 117,620 rows): the small case
-                                    for ncu captures of the fill kernel
-python bench.py --workload batch    the ragged batch of 64 radial problems
-                                    (tests/golden/ragged_problems.json): batched,
-                                    graph-captured radial stage vs the same 64
-                                    problems one handle after another
-python bench.py --workload matvec   CSR mat-vec over the singlet H blocks of the
-                                    default workload, assembled into HBM
-python bench.py --workload order9_n800
-                                    order 9, N=800, r_max=800, q=12, k=0..20,
-                                    l_max=10, singlet L=0..5: radial stage, block
-                                    counts and row samples of every block
+                [--precision fp64|mixed] [--workload order9_n800|order7_n200|...]
+python bench.py --workload order7_n200   the medium drop-in size (order 7, N=200,
+                                         k=0..10, l_max=5, L=0..3, singlet and
+                                         triplet), whole blocks into HBM
+python bench.py --profile-band B         one band fill of the large form (small
+                                         case for ncu captures of k_csr_fill)
+python bench.py --profile-block B        one whole-block fill of the medium size
+python bench.py --workload batch         the ragged batch of 64 radial problems
+python bench.py --workload matvec        CSR mat-vec over medium-size H blocks
 """
 import argparse
 import json
@@ -44,22 +52,36 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 METRIC = "R^k elements/s + 2e-H assembly s, mixed vs FP64 on GB300 at ≤1e-9 rel err"
-WORKLOAD = dict(k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5, max_L=3, Z=2, spins=(0, 1),
-                full=True, cap_order=2, cap_r0=10.0, cap_eta=1e-3)
+
+LARGE = dict(name="order9_n800", k=9, n_b=800, r_max=800.0, q=12, max_k=20, l_max=10,
+             max_L=5, Z=2, spins=(0,), dipoles=True, cap_order=2, cap_r0=10.0, cap_eta=1e-3,
+             area_bytes=24 << 30, n_chunks=16, cpu_frac=3 / 640000)
+MEDIUM = dict(name="order7_n200", k=7, n_b=200, r_max=200.0, q=10, max_k=10, l_max=5,
+              max_L=3, Z=2, spins=(0, 1), dipoles=False, cap_order=2, cap_r0=10.0,
+              cap_eta=1e-3, n_chunks=1, cpu_frac=1e-2)
+WORKLOADS = {"order9_n800": LARGE, "order7_n200": MEDIUM}
+
+# DRAM bytes per algorithmic byte of the band fill, from one ncu capture of
+# one band of the large form per precision (the figures and the command are
+# in the profile summaries kept with this repository); None until captured.
+FILL_TRAFFIC_RATIO = {"order9_n800": {"fp64": None, "mixed": None},
+                      "order7_n200": {"fp64": 3478840576.0 / 3453526224.0,
+                                      "mixed": 3683740672.0 / 3453526224.0}}
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of the k_csr_fill launch on
-# block 0 (ncu --set full, profiles/k_csr_fill_order7_n200_block0.md) and that
-# launch's algorithmic bytes (3,154,438,224 B of CSR + 20,100 staged tiles).
-NCU_BLOCK0_DRAM = {"fp64": 3478840576.0, "mixed": 3683740672.0}
-NCU_BLOCK0_ALG = 3453526224.0
+def workload_string(w):
+    """The workload as both arms print it."""
+    if w["name"] == "order9_n800":
+        return ("order 9, N=800, r_max=800, q=12, k=0..20, l_max=10, singlet L=0..5 full "
+                "blocks + dipole blocks L->L+1 (q=0, length gauge)")
+    return ("order 7, N=200, r_max=200, q=10, k=0..10, l_max=5, L=0..3 singlet+triplet full "
+            "blocks")
 
 
 def _pkg():
@@ -85,12 +107,21 @@ def band_pairs(k, n_b):
     return n_b * (2 * k - 1) - k * (k - 1)
 
 
-def workload_blocks(pkg, w):
+def rk_elements(w):
+    return band_pairs(w["k"], w["n_b"]) ** 2 * (w["max_k"] + 1)
+
+
+def tile_doubles(w):
+    return ((w["max_k"] + 1) * (2 * w["k"] - 1) ** 2 + 1) // 2 * 2
+
+
+def block_list(pkg, w):
+    """[(L, M, parity, spin, configs)] in init_basis order, singlet then triplet."""
     out = []
     for spin in w["spins"]:
         for (L, M, par) in pkg.basis.symmetries(w["max_L"], True):
-            cf = pkg.configs(L, par, w["l_max"], w["n_b"], w["k"], spin=spin)
-            out.append((L, par, spin, cf))
+            out.append((L, M, par, spin, pkg.configs(L, par, w["l_max"], w["n_b"], w["k"],
+                                                     spin=spin)))
     return out
 
 
@@ -103,6 +134,7 @@ class Clocks:
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
+        self.lines = []
 
     def __enter__(self):
         try:
@@ -147,284 +179,817 @@ class Clocks:
 
 
 # --------------------------------------------------------------------------
-# CPU baseline (oracle) on a bounded sample
+# CPU: the oracle on the same fraction f of every stage
 # --------------------------------------------------------------------------
-def cpu_baseline(pkg, w, rows_per_block=96, threads=None):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    from concurrent.futures import ThreadPoolExecutor
-    threads = threads or os.cpu_count()
-    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
-    t0 = time.perf_counter()
-    prim = O.slater(t, w["k"], w["q"], w["max_k"], nthreads=threads)
-    t1 = time.perf_counter()
-    R = O.rk_map(w["n_b"], w["k"], w["max_k"], prim)
-    t2 = time.perf_counter()
-    H1p = O.setup_H1p(t, w["k"], w["q"], w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"],
-                      w["cap_eta"])
-    S = O.setup_S(t, w["k"], w["q"])
-    blocks = [(L, par, spin, O.count_configs(L, par, w["l_max"], w["n_b"], w["k"], spin=spin))
-              for spin in w["spins"] for (L, M, par) in pkg.basis.symmetries(w["max_L"], True)]
+class CpuSample:
+    """The reference's algorithm (the oracle) on a fraction f of the job's work
+    units: f of the N^2 R^k tiles (rk_tiles: the tile's primitives and the
+    reference's summation of them), f of the rows of every symmetry block
+    (construct_block: the reference's O(n_config) loop per row) and f of the
+    rows of every dipole block (construct_dip_block_tensor per row).  The
+    one-body and radial dipole matrices (O(N k q) work) and the R^k tiles the
+    sampled rows read (the R^k stage's other units) are prepared untimed.
+    Every stage gets the same fraction, so the sample is f of the job."""
 
-    def run(b):
-        L, par, spin, cf = b
-        n = cf.size
-        starts = np.linspace(0, n - 1, rows_per_block).astype(np.int64)
-        ts = time.perf_counter()
-        for r in starts:
-            O.construct_block(cf, L, w["k"], w["n_b"], w["max_k"], R, H1p, S, w["full"], spin,
-                              rows=(int(r), int(r) + 1))
-        return (time.perf_counter() - ts) * n / rows_per_block
+    def __init__(self, pkg, w, threads=None):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+        self.O = O
+        self.pkg = pkg
+        self.w = w
+        self.threads = threads or os.cpu_count() or 1
+        self.t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+        self.blocks = block_list(pkg, w)
+        self.H1p = O.setup_H1p(self.t, w["k"], w["q"], w["Z"], w["l_max"] + 1, w["cap_order"],
+                               w["cap_r0"], w["cap_eta"])
+        self.S = O.setup_S(self.t, w["k"], w["q"])
+        self.mats = O.setup_radial_dip(self.t, w["k"], w["q"], 0) if w["dipoles"] else None
 
-    t3 = time.perf_counter()
-    with ThreadPoolExecutor(max_workers=min(threads, len(blocks))) as ex:
-        est = list(ex.map(run, blocks))
-    t4 = time.perf_counter()
-    t_full = (t1 - t0) + (t2 - t1) + max(est)
-    P = band_pairs(w["k"], w["n_b"])
-    elems = P * P * (w["max_k"] + 1)
-    return dict(value=elems / t_full, unit="R^k elements/s", cores=threads, kind="port",
-                sample=("full Slater primitives (%.1f s, OpenMP over k) + full R^k map (%.1f s, "
-                        "serial) measured; assembly extrapolated from %d evenly spaced rows of each "
-                        "of the %d blocks (%.1f s of sampling, one thread per block): full path "
-                        "%.0f s" % (t1 - t0, t2 - t1, rows_per_block, len(blocks), t4 - t3, t_full)),
-                t_full_s=t_full, t_slater_s=t1 - t0, t_rk_s=t2 - t1, t_assembly_s=max(est))
+    def _rows(self, n, f, rng):
+        m = max(1, int(round(f * n)))
+        return np.sort(rng.choice(n, size=m, replace=False)), m / n
+
+    def run(self, f, seed):
+        from concurrent.futures import ThreadPoolExecutor
+        O, w = self.O, self.w
+        N, k = w["n_b"], w["k"]
+        key = (f, seed)
+        if getattr(self, "_key", None) != key:
+            self._prep = self._prepare(f, seed)
+            self._key = key
+        tiles, jobs, dip_jobs, fracs, T, tab = self._prep
+        n_t = len(tiles)
+        # timed: f of each stage
+        t0 = time.perf_counter()
+        O.rk_tiles(self.t, k, w["q"], w["max_k"], tiles, nthreads=self.threads)
+        t1 = time.perf_counter()
+
+        def row(j):
+            cf, L, spin, r = j
+            O.construct_block(cf, L, k, N, w["max_k"], T, self.H1p, self.S, True, spin,
+                              rows=(r, r + 1), tile_of=tab)
+
+        def drow(j):
+            (L1, M1, p1, _, c1), (L2, M2, p2, _, c2), r = j
+            O.dip_block(c1[r:r + 1], (L1, M1, p1), c2, (L2, M2, p2), 0, True, k, N, 0, self.S,
+                        self.mats)
+
+        with ThreadPoolExecutor(max_workers=self.threads) as ex:
+            list(ex.map(row, jobs))
+            t2 = time.perf_counter()
+            list(ex.map(drow, dip_jobs))
+        t3 = time.perf_counter()
+        t_all = t3 - t0
+        elems = rk_elements(w)
+        return {"value": f * elems / t_all, "unit": "R^k elements/s", "cores": self.threads,
+                "kind": "port", "f": f, "t_s": t_all,
+                "sample": ("fraction f=%.3g of every stage of one job on %d host threads: %d of "
+                           "%d R^k tiles (%.2f s), %d block rows (%.2f s), %d dipole rows "
+                           "(%.2f s); per-stage fractions %.3g..%.3g; full job %.0f s at this "
+                           "rate (not measured)" %
+                           (f, self.threads, n_t, N * N, t1 - t0, len(jobs), t2 - t1,
+                            len(dip_jobs), t3 - t2, min(fracs + [n_t / N / N]),
+                            max(fracs + [n_t / N / N]), t_all / f))}
+
+    def _prepare(self, f, seed):
+        """The sample's work units and, untimed, the R^k tiles its rows read."""
+        O, w = self.O, self.w
+        N, k = w["n_b"], w["k"]
+        rng = np.random.default_rng(seed)
+        n_t = max(1, int(round(f * N * N)))
+        flat = rng.choice(N * N, size=n_t, replace=False)
+        tiles = np.stack([flat // N + 1, flat % N + 1], axis=1)
+        jobs, dip_jobs, fracs = [], [], []
+        need = set()
+        for (L, M, par, spin, cf) in self.blocks:
+            rows, fb = self._rows(cf.size, f, rng)
+            fracs.append(fb)
+            for r in rows:
+                need.add((int(cf["n1"][r]), int(cf["n2"][r])))
+                jobs.append((cf, L, spin, int(r)))
+        if w["dipoles"]:
+            singlet = [b for b in self.blocks if b[3] == 0]
+            for (b1, b2) in zip(singlet[:-1], singlet[1:]):
+                rows, fb = self._rows(b1[4].size, f, rng)
+                fracs.append(fb)
+                for r in rows:
+                    dip_jobs.append((b1, b2, int(r)))
+        need = np.array(sorted(need), dtype=np.int64)
+        T = O.rk_tiles(self.t, k, w["q"], w["max_k"], need, nthreads=self.threads)
+        tab = O.tile_table(N, need)
+        return tiles, jobs, dip_jobs, fracs, T, tab
 
 
 # --------------------------------------------------------------------------
-# GPU arm
+# GPU: the large form in bands and dipole slices
 # --------------------------------------------------------------------------
-def run_ours(args, rank, world):
+class LargeJob:
+    """The large form on one handle: planned bands and dipole slices, cut into
+    chunks; run_chunk(j) assembles chunk j into the staging area and applies
+    it to fixed vectors with the library's mat-vec."""
+
+    def __init__(self, pkg, w, prec, area, rank=0, world=1, plan=None):
+        import torch
+        self.torch = torch
+        self.pkg, self.w = pkg, w
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+        self.h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec,
+                          device=self.dev.index, stage_bytes=w["area_bytes"])
+        self.h.set_block_cache(0)
+        self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
+        self.area = area
+        self.base = area.data_ptr()
+        self.blocks = [(L, M, par, spin, self._pin(cf)) for (L, M, par, spin, cf)
+                       in block_list(pkg, w)]
+        self.radial()
+        self.plan = plan if plan is not None else self._plan(rank, world)
+        units = [u for u in self.plan["units"] if u["owner"] == rank]
+        seen = set()
+        for u in units:  # the count pass of a block runs before its first band here
+            u["count_first"] = u["kind"] == "band" and u["block"] not in seen
+            if u["kind"] == "band":
+                seen.add(u["block"])
+        self.chunks = self._chunks(units, w["n_chunks"])
+        g = torch.Generator(device="cpu").manual_seed(7)
+        self.x = [torch.randn(cf.size, dtype=torch.complex128, generator=g).to(self.dev)
+                  for (*_, cf) in self.blocks]
+        maxr = max([u["rows"] for u in units] + [1])
+        self.y = torch.empty(maxr, dtype=torch.complex128, device=self.dev)
+        self.ysum = torch.zeros((), dtype=torch.complex128, device=self.dev)
+        torch.cuda.synchronize()
+
+    def _pin(self, cf):
+        t = self.torch.from_numpy(cf.view(np.int64).reshape(-1).copy()).pin_memory()
+        self._pinned = getattr(self, "_pinned", []) + [t]
+        return t.numpy().view(self.pkg.CONFIG_DTYPE).reshape(-1)
+
+    def radial(self):
+        w, h = self.w, self.h
+        h.slater()
+        h.rk()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+        if w["dipoles"]:
+            h.radial_dipole(0, copy_out=False)
+
+    def _plan(self, rank, world):
+        pkg, w, h = self.pkg, self.w, self.h
+        N = w["n_b"]
+        per, tiles = [], []
+        for (L, M, par, spin, cf) in self.blocks:
+            r, nh, ns, p = h.band_count(cf, L, 1, N, True, spin, per_n1=True)
+            per.append(p)
+            # staged tiles per n1: distinct (n1, n2) of the block's rows
+            key = np.unique(cf["n1"].astype(np.int64) * (N + 1) + cf["n2"])
+            tiles.append(np.bincount(key // (N + 1), minlength=N + 1)[1:])
+        # room for 256-byte alignment of six arrays and a rows list per band
+        bands = pkg.band_plan(per, w["area_bytes"] - (64 << 20), world)
+        units = []
+        for (b, a, m, owner, nbytes) in bands:
+            p = per[b][a - 1:a - 1 + m]
+            units.append(dict(kind="band", block=int(b), n1=int(a), m=int(m), owner=int(owner),
+                              bytes=int(nbytes), rows=int(p[:, 0].sum()),
+                              nH=int(p[:, 1].sum()), nS=int(p[:, 2].sum()),
+                              tiles=int(tiles[b][a - 1:a - 1 + m].sum())))
+        if w["dipoles"]:
+            load = np.zeros(world)
+            for u in units:
+                load[u["owner"]] += u["bytes"]
+            singlet = [i for i, b in enumerate(self.blocks) if b[3] == 0]
+            dips = []
+            for i1, i2 in zip(singlet[:-1], singlet[1:]):
+                dips += self._dip_slices(i1, i2)
+            for d in sorted(dips, key=lambda d: -d["bytes"]):
+                d["owner"] = int(np.argmin(load))
+                load[d["owner"]] += d["bytes"]
+            units += dips
+        return {"units": units}
+
+    def _dip_slices(self, i1, i2):
+        """Row slices of the dipole block (i1 -> i2) whose CSR fits the area."""
+        h, w = self.h, self.w
+        (L1, M1, p1, _, c1), (L2, M2, p2, _, c2) = self.blocks[i1], self.blocks[i2]
+        cap = w["area_bytes"] - (1 << 20)
+        out, todo = [], [(0, c1.size)]
+        total = h.dip_block_count(c1, (L1, M1, p1), c2, (L2, M2, p2), 0)
+        if total:
+            step = max(1, int(c1.size * 0.8 * cap / (24 * total + 8 * c1.size)))
+            todo = [(r, min(r + step, c1.size)) for r in range(0, c1.size, step)]
+        while todo:
+            r0, r1 = todo.pop(0)
+            n = h.dip_block_count(c1[r0:r1], (L1, M1, p1), c2, (L2, M2, p2), 0)
+            nbytes = 24 * n + 8 * (r1 - r0 + 1) + 512
+            if nbytes > cap and r1 - r0 > 1:
+                mid = (r0 + r1) // 2
+                todo[:0] = [(r0, mid), (mid, r1)]
+                continue
+            out.append(dict(kind="dip", block=i1, block2=i2, r0=r0, r1=r1, rows=r1 - r0,
+                            nnz=int(n), bytes=int(nbytes), owner=0))
+        return out
+
+    @staticmethod
+    def _chunks(units, n):
+        total = sum(u["bytes"] for u in units)
+        out, cur, acc = [], [], 0
+        for u in units:
+            cur.append(u)
+            acc += u["bytes"]
+            if acc >= total * (len(out) + 1) / n and len(out) < n - 1:
+                out.append(cur)
+                cur = []
+        out.append(cur)
+        while len(out) < n:
+            out.append([])
+        return out
+
+    def chunk_bytes(self, j):
+        return sum(u["bytes"] for u in self.chunks[j])
+
+    def _layout(self, parts):
+        """Device addresses of consecutive arrays in the area (256-byte aligned)."""
+        out, off = [], 0
+        for nbytes in parts:
+            out.append(self.base + off)
+            off += (int(nbytes) + 255) // 256 * 256
+        assert off <= self.area.numel() * self.area.element_size()
+        return out
+
+    def run_chunk(self, j, timers=None):
+        """Chunk j on the device; timers: dict of lists of (event, event) pairs."""
+        torch, h = self.torch, self.h
+        ev = (lambda: torch.cuda.Event(enable_timing=True)) if timers is not None else None
+
+        def mark(name, e0):
+            if timers is not None:
+                e1 = ev()
+                e1.record(self.stream)
+                timers.setdefault(name, []).append((e0, e1))
+
+        def start():
+            if timers is None:
+                return None
+            e = ev()
+            e.record(self.stream)
+            return e
+
+        if j == 0:
+            e0 = start()
+            self.radial()
+            mark("radial", e0)
+        for u in self.chunks[j]:
+            if u["kind"] == "band":
+                L, M, par, spin, cf = self.blocks[u["block"]]
+                if u["count_first"]:
+                    e0 = start()
+                    h.block_count(cf, L, True, spin)
+                    mark("count", e0)
+                r, nH, nS = u["rows"], u["nH"], u["nS"]
+                Hp, Hi, Hd, Sp, Si, Sd = self._layout([8 * (r + 1), 8 * nH, 16 * nH,
+                                                       8 * (r + 1), 8 * nS, 16 * nS])
+                e0 = start()
+                h.band_into(cf, L, u["n1"], u["m"], True, spin,
+                            dict(index_ptr=Hp, indices=Hi, data=Hd),
+                            dict(index_ptr=Sp, indices=Si, data=Sd))
+                mark("fill", e0)
+                e0 = start()
+                x, y = self.x[u["block"]].data_ptr(), self.y.data_ptr()
+                h.csr_mv_device(0, r, cf.size, nH, Hp, Hi, Hd, x, y)
+                self._acc(r)
+                h.csr_mv_device(0, r, cf.size, nS, Sp, Si, Sd, x, y)
+                self._acc(r)
+                mark("consume", e0)
+            else:
+                L1, M1, p1, _, c1 = self.blocks[u["block"]]
+                L2, M2, p2, _, c2 = self.blocks[u["block2"]]
+                rows = c1[u["r0"]:u["r1"]]
+                e0 = start()
+                n = h.dip_block_count(rows, (L1, M1, p1), c2, (L2, M2, p2), 0)
+                assert n == u["nnz"]
+                Dp, Di, Dd = self._layout([8 * (u["rows"] + 1), 8 * n, 16 * n])
+                h.dip_block_into(rows, (L1, M1, p1), c2, (L2, M2, p2), 0,
+                                 dict(index_ptr=Dp, indices=Di, data=Dd))
+                mark("dipole", e0)
+                e0 = start()
+                h.csr_mv_device(0, u["rows"], c2.size, n, Dp, Di, Dd,
+                                self.x[u["block2"]].data_ptr(), self.y.data_ptr())
+                self._acc(u["rows"])
+                mark("consume", e0)
+
+    def _acc(self, r):
+        with self.torch.cuda.stream(self.stream):
+            self.ysum += self.y[:r].sum()
+
+    def band_sample(self, u):
+        """Device copy of one band's H data (for precision comparisons)."""
+        torch, h = self.torch, self.h
+        L, M, par, spin, cf = self.blocks[u["block"]]
+        r, nH, nS = u["rows"], u["nH"], u["nS"]
+        Hp, Hi, Hd, Sp, Si, Sd = self._layout([8 * (r + 1), 8 * nH, 16 * nH, 8 * (r + 1),
+                                               8 * nS, 16 * nS])
+        h.band_into(cf, L, u["n1"], u["m"], True, spin, dict(index_ptr=Hp, indices=Hi, data=Hd),
+                    dict(index_ptr=Sp, indices=Si, data=Sd))
+        off = (8 * (r + 1) + 255) // 256 * 256 + (8 * nH + 255) // 256 * 256
+        data = self.area.view(torch.uint8)[off:off + 16 * nH].view(torch.complex128)
+        return data.clone()
+
+    def e2e_chunk(self, j, host):
+        """Chunk j through the C ABI with host outputs (pinned buffers in host);
+        returns (h2d bytes, d2h bytes)."""
+        h = self.h
+        h2d = d2h = 0
+        if j == 0:
+            self.radial()
+            h2d += self.h.knots.nbytes
+        for u in self.chunks[j]:
+            if u["kind"] == "band":
+                L, M, par, spin, cf = self.blocks[u["block"]]
+                if u["count_first"]:
+                    h.block_count(cf, L, True, spin)
+                    h2d += cf.nbytes
+                r, nH, nS = u["rows"], u["nH"], u["nS"]
+                H = dict(index_ptr=host["ptrH"][:r + 1], indices=host["idxH"][:nH],
+                         data=host["datH"][:nH])
+                S = dict(index_ptr=host["ptrS"][:r + 1], indices=host["idxS"][:nS],
+                         data=host["datS"][:nS])
+                h.band_host_into(cf, L, u["n1"], u["m"], True, spin, H, S, host["rows"][:r])
+                h2d += cf.nbytes
+                d2h += 24 * (nH + nS) + 16 * (r + 1) + 8 * r
+            else:
+                L1, M1, p1, _, c1 = self.blocks[u["block"]]
+                L2, M2, p2, _, c2 = self.blocks[u["block2"]]
+                rows = c1[u["r0"]:u["r1"]]
+                n = h.dip_block_count(rows, (L1, M1, p1), c2, (L2, M2, p2), 0)
+                D = dict(index_ptr=host["ptrH"][:u["rows"] + 1], indices=host["idxH"][:n],
+                         data=host["datH"][:n])
+                self.pkg.lib().bs2e_dip_block_fill(
+                    h._h, self.pkg._ptr(rows), rows.size, L1, M1, p1, self.pkg._ptr(c2), c2.size,
+                    L2, M2, p2, 0, 1, self.pkg._ptr(D["index_ptr"]), self.pkg._ptr(D["indices"]),
+                    self.pkg._ptr(D["data"]), 0)
+                h2d += 2 * (rows.nbytes + c2.nbytes)
+                d2h += 24 * n + 8 * (u["rows"] + 1)
+        return h2d, d2h
+
+    def close(self):
+        self.h.close()
+
+
+def run_large(args, rank, world):
     import torch
     pkg = _pkg()
-    w = WORKLOAD
+    w = LARGE
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
-    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
-    blocks = workload_blocks(pkg, w)
-    h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec, device=dev.index)
-    stream = torch.cuda.ExternalStream(h.stream, device=dev)
+    area = torch.empty(w["area_bytes"] // 8, dtype=torch.float64, device=dev)
+    prec_main = args.precision
+    precs = {"fp64": pkg.PREC_FP64, "mixed": pkg.PREC_MIXED}
+    job = LargeJob(pkg, w, precs[prec_main], area, rank, world)
+    nc = w["n_chunks"]
+    elems = rk_elements(w)
+    total_bytes = sum(u["bytes"] for u in job.plan["units"])
+    # warm-up
+    for s in range(args.warmup):
+        job.run_chunk(s % nc)
+    _barrier(world)
+    launches0 = job.h.launch_count
+    timers = {}
+    step_ev = []
+    with Clocks(dev.index) as clk:
+        _barrier(world)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev0.record(job.stream)
+        for s in range(args.steps):
+            e = torch.cuda.Event(enable_timing=True)
+            job.run_chunk(s % nc, timers)
+            e.record(job.stream)
+            step_ev.append(e)
+        torch.cuda.synchronize()
+        _barrier(world)
+    launches = job.h.launch_count - launches0
+    t_steps = [ev0.elapsed_time(step_ev[0]) / 1e3] + [
+        step_ev[i - 1].elapsed_time(step_ev[i]) / 1e3 for i in range(1, len(step_ev))]
+    t_dev = _max_over_ranks(sum(t_steps), world)
+    done_bytes = sum(job.chunk_bytes(s % nc) for s in range(args.steps))
+    done_bytes = _sum_over_ranks(done_bytes, world)
+    jobs_done = done_bytes / total_bytes
+    value = elems * jobs_done / t_dev
+    job_s = sum(t_steps[:nc]) if args.steps >= nc else None
+    job_s = _max_over_ranks(job_s, world) if job_s is not None else None
+    sums = {k: sum(a.elapsed_time(b) for a, b in v) / 1e3 for k, v in timers.items()}
+    n_jobs_local = args.steps / nc
+    fill_units = [u for j in range(args.steps) for u in job.chunks[j % nc] if u["kind"] == "band"]
+    tile_b = 8 * tile_doubles(w)
+    fill_bytes = sum(24 * (u["nH"] + u["nS"]) + 16 * (u["rows"] + 1) + tile_b * u["tiles"]
+                     for u in fill_units)
+    peak, peak_src = _peaks()
+    achieved = fill_bytes / sums["fill"] / 1e9 if sums.get("fill") else None
+    ratio = FILL_TRAFFIC_RATIO["order9_n800"][prec_main]
+    per_launch = fill_bytes / max(len(fill_units), 1)
+    res = {
+        "metric": METRIC, "value": value, "unit": "R^k elements/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "strong", "vs_baseline": None,
+        "dtype": "f64" if prec_main == "fp64" else "f64 out, f32-pair k-sum",
+        "data": "synthetic (deterministic knot grid, no dataset)",
+        "config": {"workload": workload_string(w), "precision": prec_main,
+                   "step": "1/%d of a job: %d bands of 6 blocks and %d dipole row slices cut "
+                           "into %d chunks of nearly equal CSR bytes, chunk 0 with the radial "
+                           "stage" % (nc, sum(u["kind"] == "band" for u in job.plan["units"]),
+                                      sum(u["kind"] == "dip" for u in job.plan["units"]), nc),
+                   "rk_elements_per_job": elems, "csr_bytes_per_job": total_bytes,
+                   "rows": [int(b[4].size) for b in job.blocks],
+                   "nnz_H_S_per_job": sum(u.get("nH", 0) + u.get("nS", 0)
+                                          for u in job.plan["units"]),
+                   "nnz_dipole_per_job": sum(u.get("nnz", 0) for u in job.plan["units"]),
+                   "l2": "every step writes ~%.0f GB of CSR (> L2)" % (total_bytes / nc / 1e9),
+                   "consumer": "bs2e_csr_mv of every band of H and S and slice of D with a "
+                               "fixed vector, on the device"},
+        "job_s": job_s, "jobs_timed": jobs_done,
+        "assembly_s_per_job": (sums.get("fill", 0) + sums.get("dipole", 0) + sums.get("count", 0))
+                              / n_jobs_local,
+        "radial_s": sums.get("radial", 0) / max(1, sum(1 for s in range(args.steps) if s % nc == 0)),
+        "consume_s_per_job": sums.get("consume", 0) / n_jobs_local,
+        "rk_stage_elements_per_s": None,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_csr_fill (band fills)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": ratio * per_launch if ratio else None, "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": per_launch, "launches": len(fill_units),
+                     "note": "achieved = (24 B per H/S entry + pointers + staged R^k tiles) / "
+                             "CUDA-event time of the band-fill calls on the library stream"},
+        "clocks": clk.summary(),
+        "checksum_y": complex(job.ysum.item()).__repr__(),
+    }
+    if res["radial_s"]:
+        res["rk_stage_elements_per_s"] = elems / res["radial_s"]
+    # mixed vs FP64: the other precision over one whole job, and errors on sampled bands
+    if not args.no_mixed and world == 1:
+        other = "mixed" if prec_main == "fp64" else "fp64"
+        samples = _sample_units(job)
+        ref = [job.band_sample(u) for u in samples]
+        job.close()
+        torch.cuda.empty_cache()
+        job2 = LargeJob(pkg, w, precs[other], area, rank, world, plan=job.plan)
+        job2.run_chunk(0)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(job2.stream)
+        for j in range(nc):
+            job2.run_chunk(j)
+        t1.record(job2.stream)
+        torch.cuda.synchronize()
+        got = [job2.band_sample(u) for u in samples]
+        err = _compare(ref, got) if prec_main == "fp64" else _compare(got, ref)
+        t_other = t0.elapsed_time(t1) / 1e3
+        res["mixed_vs_fp64"] = {
+            other + "_job_s": t_other, prec_main + "_job_s": job_s,
+            "mixed_speedup_vs_fp64": ((job_s / t_other) if prec_main == "fp64" else
+                                      (t_other / job_s)) if job_s else None,
+            "errors_mixed_vs_fp64": err,
+            "sampled_bands": [(u["block"], u["n1"], u["m"], u["nH"]) for u in samples]}
+        job2.close()
+        torch.cuda.empty_cache()
+        job = LargeJob(pkg, w, precs[prec_main], area, rank, world, plan=job.plan)
+    if not args.no_e2e and world == 1:
+        res["e2e"] = _e2e_large(job, args, elems, total_bytes)
+    job.close()
+    del area
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cs = CpuSample(pkg, w).run(w["cpu_frac"], seed=1)
+        res["cpu_baseline"] = {k: v for k, v in cs.items()
+                               if k in ("value", "unit", "cores", "kind", "sample")}
+    return res
 
-    def radial():
+
+def _sample_units(job, nmax=6, max_bytes=2 << 30):
+    """Small bands, one per block where one exists."""
+    out = []
+    for b in range(len(job.blocks)):
+        cands = [u for u in job.plan["units"] if u["kind"] == "band" and u["block"] == b and
+                 u["bytes"] <= max_bytes]
+        if cands:
+            out.append(min(cands, key=lambda u: u["bytes"]))
+    return out[:nmax]
+
+
+def _compare(fp64_list, mixed_list, floor=1e-15):
+    """Mixed vs FP64 on the same bands: per entry (entries >= floor Eh) and
+    relative to the band's largest |entry|."""
+    import torch
+    e_max = e_ms = m_max = 0.0
+    n = n_below = 0
+    for a, b in zip(fp64_list, mixed_list):
+        if a.numel() == 0:
+            continue
+        d = (b - a).abs()
+        aa = a.abs()
+        top = float(aa.max())
+        mask = aa >= floor
+        if mask.any():
+            r = d[mask] / aa[mask]
+            e_max = max(e_max, float(r.max()))
+            e_ms += float((r * r).sum())
+            n += int(mask.sum())
+        n_below += int((~mask).sum())
+        if top > 0:
+            m_max = max(m_max, float(d.max()) / top)
+        del d, aa, mask
+    torch.cuda.empty_cache()
+    return {"entry_max": e_max, "entry_rms": (e_ms / n) ** 0.5 if n else 0.0,
+            "entry_floor_eh": floor, "entries": n, "entries_below_floor": n_below,
+            "rel_to_band_max_max": m_max,
+            "note": "per entry over entries >= the floor; a cancelling entry (terms summing "
+                    "to far below their magnitudes) shows the terms' rounding magnified, "
+                    "see the oracle parity tests for the term-scale figures"}
+
+
+def _e2e_large(job, args, elems, total_bytes):
+    import torch
+    nc = len(job.chunks)
+    maxH = max([u.get("nH", u.get("nnz", 0)) for u in job.plan["units"]] + [1])
+    maxS = max([u.get("nS", 0) for u in job.plan["units"]] + [1])
+    maxr = max([u["rows"] for u in job.plan["units"]] + [1])
+    pin = lambda n, dt: torch.empty(int(n), dtype=dt, pin_memory=True).numpy()
+    host = dict(ptrH=pin(maxr + 1, torch.int64), idxH=pin(maxH, torch.int64),
+                datH=pin(maxH, torch.complex128), ptrS=pin(maxr + 1, torch.int64),
+                idxS=pin(maxS, torch.int64), datS=pin(maxS, torch.complex128),
+                rows=pin(maxr, torch.int64))
+    n = max(1, min(args.e2e_steps, nc))
+    job.e2e_chunk(0, host)  # warm (first-touch of the pinned pages)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    done = 0
+    for j in range(n):
+        a, b = job.e2e_chunk(j, host)
+        h2d += a
+        d2h += b
+        done += job.chunk_bytes(j)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    return {"value": elems * (done / total_bytes) / t, "unit": "R^k elements/s",
+            "h2d_bytes_per_step": int(h2d / n), "d2h_bytes_per_step": int(d2h / n),
+            "steps": n, "s_per_step": t / n, "d2h_achieved_gbs": d2h / t / 1e9,
+            "timing": "wall clock, chunks 0..%d (chunk 0 with the radial stage)" % (n - 1)}
+
+
+# --------------------------------------------------------------------------
+# GPU: the medium size, whole blocks into HBM
+# --------------------------------------------------------------------------
+def run_medium(args, rank, world):
+    import torch
+    pkg = _pkg()
+    w = MEDIUM
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    precs = {"fp64": pkg.PREC_FP64, "mixed": pkg.PREC_MIXED}
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    blocks = block_list(pkg, w)
+    work = [pkg.basis.block_work(cf.size, len(set(zip(cf["l1"], cf["l2"]))))
+            for (*_, cf) in blocks]
+    mine = pkg.basis.shard_blocks(work, world, rank)
+    elems = rk_elements(w)
+
+    def make(prec):
+        h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=precs[prec], device=dev.index)
+        h.set_block_cache(0)
+        return h
+
+    def radial(h):
         h.slater()
         h.rk()
         h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
                    copy_out=False)
 
-    radial()
-    counts = [h.block_count(cf, L, w["full"], spin) for (L, par, spin, cf) in blocks]
-    nH = sum(c[0] for c in counts)
-    nS = sum(c[1] for c in counts)
-    # device-resident outputs for every block
-    out_dev = []
-    for (L, par, spin, cf), (ch, cs) in zip(blocks, counts):
-        n = cf.size
-        Hd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
-                  indices=torch.empty(ch, dtype=torch.int64, device=dev),
-                  data=torch.empty(ch, dtype=torch.complex128, device=dev))
-        Sd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
-                  indices=torch.empty(cs, dtype=torch.int64, device=dev),
-                  data=torch.empty(cs, dtype=torch.complex128, device=dev))
-        out_dev.append((Hd, Sd))
-    ptrs = [({x: v.data_ptr() for x, v in Hd.items()}, {x: v.data_ptr() for x, v in Sd.items()})
-            for (Hd, Sd) in out_dev]
-    tile_bytes = 8 * ((w["max_k"] + 1) * (2 * w["k"] - 1) ** 2 + 1) // 2 * 2
-    n_tiles = sum(np.unique(cf["n1"] * 100000 + cf["n2"]).size for (_, _, _, cf) in blocks)
-    fill_bytes = 24 * (nH + nS) + n_tiles * tile_bytes
+    h = make(args.precision)
+    stream = torch.cuda.ExternalStream(h.stream, device=dev)
+    radial(h)
+    counts = {i: h.block_count(blocks[i][4], blocks[i][0], True, blocks[i][3]) for i in mine}
+    out_dev = {}
+    for i in mine:
+        n = blocks[i][4].size
+        ch, cs = counts[i]
+        mk = lambda m, dt: torch.empty(max(int(m), 1), dtype=dt, device=dev)
+        out_dev[i] = (dict(index_ptr=mk(n + 1, torch.int64), indices=mk(ch, torch.int64),
+                           data=mk(ch, torch.complex128)),
+                      dict(index_ptr=mk(n + 1, torch.int64), indices=mk(cs, torch.int64),
+                           data=mk(cs, torch.complex128)))
+    ptrs = {i: ({x: v.data_ptr() for x, v in a.items()}, {x: v.data_ptr() for x, v in b.items()})
+            for i, (a, b) in out_dev.items()}
+    tile_b = 8 * tile_doubles(w)
+    n_tiles = sum(np.unique(blocks[i][4]["n1"] * 100000 + blocks[i][4]["n2"]).size for i in mine)
+    fill_bytes = 24 * sum(a + b for a, b in counts.values()) + n_tiles * tile_b
 
-    fill_ms = []
-
-    def step_device(record):
-        radial()
-        for b, ((L, par, spin, cf), (Hp, Sp)) in enumerate(zip(blocks, ptrs)):
-            h.block_count(cf, L, w["full"], spin)
-            if record:
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-            h.block_fill_into(cf, L, w["full"], spin, Hp, Sp, on_device=True)
-            if record:
-                e1.record(stream)
-                fill_ms.append((e0, e1))
-
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+    def step(hh, pp, timers=None):
+        e = lambda: torch.cuda.Event(enable_timing=True)
+        if timers is not None:
+            r0 = e()
+            r0.record(stream)
+        radial(hh)
+        if timers is not None:
+            r1 = e()
+            r1.record(stream)
+            timers.setdefault("radial", []).append((r0, r1))
+        for i in mine:
+            L, M, par, spin, cf = blocks[i]
+            hh.block_count(cf, L, True, spin)  # the count pass (no block cache)
+            if timers is not None:
+                f0 = e()
+                f0.record(stream)
+            hh.block_fill_into(cf, L, True, spin, pp[i][0], pp[i][1], on_device=True)
+            if timers is not None:
+                f1 = e()
+                f1.record(stream)
+                timers.setdefault("fill", []).append((f0, f1))
 
     for _ in range(args.warmup):
-        step_device(False)
-    barrier()
+        step(h, ptrs)
+    _barrier(world)
     launches0 = h.launch_count
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
+    timers = {}
     with Clocks(dev.index) as clk:
-        barrier()
+        _barrier(world)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         for _ in range(args.steps):
-            step_device(True)
+            step(h, ptrs, timers)
         ev1.record(stream)
-        barrier()
+        torch.cuda.synchronize()
+        _barrier(world)
     launches = h.launch_count - launches0
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    fill_s = sum(a.elapsed_time(b) for a, b in fill_ms) / 1e3
-    nb = len(blocks)
-    per_block_ms = [sum(fill_ms[i][0].elapsed_time(fill_ms[i][1])
-                        for i in range(j, len(fill_ms), nb)) / args.steps for j in range(nb)]
-    t_dev = _max_over_ranks(t_dev, world)
-    P = band_pairs(w["k"], w["n_b"])
-    elems = P * P * (w["max_k"] + 1)
-    value = world * elems * args.steps / t_dev
-    # radial stage alone (slater + R^k + one-body), for the "+ 2e-H assembly s" split
-    barrier()
-    r0 = torch.cuda.Event(enable_timing=True)
-    r1 = torch.cuda.Event(enable_timing=True)
-    r0.record(stream)
-    for _ in range(args.steps):
-        radial()
-    r1.record(stream)
-    barrier()
-    t_radial = r0.elapsed_time(r1) / 1e3 / args.steps
-
-    if args.no_e2e:
-        return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, None,
-                       launches, fill_bytes, fill_s, clk, h, rank, per_block_ms)
-    # e2e through the C ABI with pinned host buffers
-    del out_dev
-    torch.cuda.empty_cache()
-    host = []
-    for (L, par, spin, cf), (ch, cs) in zip(blocks, counts):
-        n = cf.size
-        mk = lambda m, dt: torch.empty(m, dtype=dt, pin_memory=True).numpy()
-        H = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(ch, torch.int64),
-                 data=mk(ch, torch.complex128))
-        S = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(cs, torch.int64),
-                 data=mk(cs, torch.complex128))
-        host.append((H, S))
-    pinned_cfg = [torch.from_numpy(cf.view(np.int64).copy()).pin_memory().numpy().view(
-        pkg.CONFIG_DTYPE) for (_, _, _, cf) in blocks]
-    h2d = t.nbytes + sum(c.nbytes for c in pinned_cfg)
-    d2h = sum(H["index_ptr"].nbytes + H["indices"].nbytes + H["data"].nbytes +
-              S["index_ptr"].nbytes + S["indices"].nbytes + S["data"].nbytes for H, S in host)
-
-    def step_e2e():
-        radial()
-        for (L, par, spin, _), cf, (H, S) in zip(blocks, pinned_cfg, host):
-            h.block_count(cf, L, w["full"], spin)
-            h.block_fill_into(cf, L, w["full"], spin, H, S, on_device=False)
-
-    e2e_steps = max(1, min(args.steps, 3))
-    step_e2e()
-    barrier()
-    te0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        step_e2e()
-    barrier()
-    t_e2e = _max_over_ranks((time.perf_counter() - te0) / e2e_steps, world)
-    # this box's device-to-host copy rate into the same pinned buffers: one
-    # 4 GiB copy into the largest, and copies covering every byte of all of
-    # them (the ceiling of the e2e number, which depends on the host pages)
-    big = max((x for H, S in host for x in (H["data"], S["data"])), key=lambda a: a.nbytes)
-    nbytes = min(big.nbytes, 4 << 30) // 16 * 16
-    src = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
-    dst = torch.from_numpy(big.view(np.float64)[:nbytes // 8])
-    dst.copy_(src, non_blocking=True)
-    torch.cuda.synchronize()
-    tc0 = time.perf_counter()
-    for _ in range(3):
-        dst.copy_(src, non_blocking=True)
-    torch.cuda.synchronize()
-    d2h_gbs = 3 * nbytes / (time.perf_counter() - tc0) / 1e9
-    srcb = src.view(torch.uint8)
-    tc0 = time.perf_counter()
-    tot_b = 0
-    for H, S in host:
-        for a in (H["index_ptr"], H["indices"], H["data"], S["index_ptr"], S["indices"], S["data"]):
-            flat = torch.from_numpy(a.view(np.uint8).reshape(-1))
-            for o in range(0, flat.numel(), nbytes):
-                m = min(nbytes, flat.numel() - o)
-                flat[o:o + m].copy_(srcb[:m], non_blocking=True)
-                tot_b += m
-    torch.cuda.synchronize()
-    d2h_all_gbs = tot_b / (time.perf_counter() - tc0) / 1e9
-    del src, srcb
-    e2e = {"value": world * elems / t_e2e, "unit": "R^k elements/s",
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "s_per_step": t_e2e,
-           "d2h_copy_gbs_this_box": d2h_gbs, "d2h_copy_gbs_all_buffers": d2h_all_gbs,
-           "d2h_achieved_gbs": d2h / t_e2e / 1e9}
-    return _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
-                   fill_bytes, fill_s, clk, h, rank, per_block_ms)
-
-
-def _result(args, pkg, prec, world, blocks, nH, nS, elems, t_dev, t_radial, e2e, launches,
-            fill_bytes, fill_s, clk, h, rank, per_block_ms):
-    w = WORKLOAD
-    value = world * elems * args.steps / t_dev
+    t_dev = _max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    sums = {k: sum(a.elapsed_time(b) for a, b in v) / 1e3 for k, v in timers.items()}
+    value = elems * args.steps / t_dev
     peak, peak_src = _peaks()
-    achieved = fill_bytes * args.steps / fill_s / 1e9 if fill_s > 0 else None
-    # DRAM bytes of an average fill launch: block 0's measured traffic per
-    # algorithmic byte times the average launch's algorithmic bytes
-    traffic = NCU_BLOCK0_DRAM[args.precision] / NCU_BLOCK0_ALG * fill_bytes / len(blocks)
+    achieved = fill_bytes * args.steps / sums["fill"] / 1e9 if sums.get("fill") else None
+    ratio = FILL_TRAFFIC_RATIO["order7_n200"][args.precision]
     res = {
         "metric": METRIC, "value": value, "unit": "R^k elements/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == pkg.PREC_FP64 else "f64 out, f32-pair k-sum",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f64 out, f32-pair k-sum",
         "data": "synthetic (deterministic knot grid, no dataset)",
-        "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 "
-                               "singlet+triplet full blocks (8 blocks, %d rows)" %
-                               sum(cf.size for (_, _, _, cf) in blocks),
-                   "precision": args.precision, "nnz_H": nH, "nnz_S": nS,
-                   "rk_elements_per_step": elems,
-                   "l2": "every step writes %.1f GB of CSR (> L2)" % (24 * (nH + nS) / 1e9)},
-        "assembly_s": (t_dev / args.steps) - t_radial,
-        "radial_s": t_radial,
-        "rk_stage_elements_per_s": elems / t_radial,
-        "e2e": e2e,
+        "config": {"workload": workload_string(w), "precision": args.precision,
+                   "blocks_this_rank": mine, "rk_elements_per_step": elems,
+                   "nnz_H_S": int(sum(a + b for a, b in counts.values())),
+                   "l2": "every step writes %.1f GB of CSR (> L2)" %
+                         (24 * sum(a + b for a, b in counts.values()) / 1e9)},
+        "assembly_s": t_dev / args.steps - sums.get("radial", 0) / args.steps,
+        "radial_s": sums.get("radial", 0) / args.steps,
+        "rk_stage_elements_per_s": elems / (sums["radial"] / args.steps) if sums.get("radial") else None,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "k_csr_fill", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic, "peak_source": peak_src,
-                     "algorithmic_bytes_per_launch": fill_bytes / len(blocks),
-                     "launches_per_step": len(blocks),
-                     "fill_s_per_step": fill_s / args.steps,
-                     "fill_ms_per_block": per_block_ms},
+                     "traffic": ratio * fill_bytes / max(len(mine), 1), "peak_source": peak_src,
+                     "algorithmic_bytes_per_launch": fill_bytes / max(len(mine), 1),
+                     "launches_per_step": len(mine), "fill_s_per_step": sums.get("fill", 0) / args.steps},
         "clocks": clk.summary(),
     }
+    if not args.no_mixed and world == 1:
+        other = "mixed" if args.precision == "fp64" else "fp64"
+        sel = [i for i in mine if blocks[i][0] == 0]
+        ref = {i: out_dev[i][0]["data"][:counts[i][0]].clone() for i in sel}
+        h2 = make(other)
+        for _ in range(2):
+            step(h2, ptrs)
+        torch.cuda.synchronize()
+        s2 = torch.cuda.ExternalStream(h2.stream, device=dev)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(s2)
+        n2 = max(2, min(args.steps, 5))
+        for _ in range(n2):
+            step(h2, ptrs)
+        a1.record(s2)
+        torch.cuda.synchronize()
+        got = {i: out_dev[i][0]["data"][:counts[i][0]].clone() for i in sel}
+        pair = ([ref[i] for i in sel], [got[i] for i in sel])
+        err = _compare(*pair) if args.precision == "fp64" else _compare(pair[1], pair[0])
+        t2 = a0.elapsed_time(a1) / 1e3 / n2
+        res["mixed_vs_fp64"] = {other + "_ms_per_step": 1e3 * t2,
+                                args.precision + "_ms_per_step": 1e3 * t_dev / args.steps,
+                                "mixed_speedup_vs_fp64": (t_dev / args.steps / t2)
+                                if args.precision == "fp64" else (t2 / (t_dev / args.steps)),
+                                "errors_mixed_vs_fp64": err,
+                                "compared": "every H entry of the L=0 blocks"}
+        h2.close()
+        del ref, got
+    if not args.no_e2e and world == 1:
+        del out_dev
+        torch.cuda.empty_cache()
+        res["e2e"] = _e2e_medium(h, pkg, w, blocks, mine, counts, args, elems, t, radial)
     h.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        res["cpu_baseline"] = {k: v for k, v in cpu_baseline(pkg, w).items()
+        cs = CpuSample(pkg, w).run(w["cpu_frac"], seed=1)
+        res["cpu_baseline"] = {k: v for k, v in cs.items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
     return res
 
 
-def profile_block(args):
-    """Small case for ncu: one radial pass, then count + fill of one block into
-    device buffers (block 0 writes ~2.9 GB of CSR, above L2, one k_fill launch)."""
+def _e2e_medium(h, pkg, w, blocks, mine, counts, args, elems, t, radial):
+    import torch
+    host = {}
+    for i in mine:
+        n = blocks[i][4].size
+        ch, cs = counts[i]
+        mk = lambda m, dt: torch.empty(max(int(m), 1), dtype=dt, pin_memory=True).numpy()
+        host[i] = (dict(index_ptr=mk(n + 1, torch.int64), indices=mk(ch, torch.int64),
+                        data=mk(ch, torch.complex128)),
+                   dict(index_ptr=mk(n + 1, torch.int64), indices=mk(cs, torch.int64),
+                        data=mk(cs, torch.complex128)))
+    pinned_cfg = {i: torch.from_numpy(blocks[i][4].view(np.int64).copy()).pin_memory().numpy()
+                  .view(pkg.CONFIG_DTYPE) for i in mine}
+    h2d = t.nbytes + sum(c.nbytes for c in pinned_cfg.values())
+    d2h = sum(sum(a.nbytes for a in H.values()) + sum(a.nbytes for a in S.values())
+              for H, S in host.values())
+
+    def step():
+        radial(h)
+        for i in mine:
+            L, M, par, spin, _ = blocks[i]
+            h.block_count(pinned_cfg[i], L, True, spin)
+            h.block_fill_into(pinned_cfg[i], L, True, spin, host[i][0], host[i][1],
+                              on_device=False)
+
+    n = max(1, min(args.steps, args.e2e_steps))
+    step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(n):
+        step()
+    torch.cuda.synchronize()
+    te = (time.perf_counter() - t0) / n
+    return {"value": elems / te, "unit": "R^k elements/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "s_per_step": te, "steps": n,
+            "d2h_achieved_gbs": d2h / te / 1e9}
+
+
+# --------------------------------------------------------------------------
+# small cases for ncu, the ragged batch and the mat-vec
+# --------------------------------------------------------------------------
+def profile_band(args):
+    """One band fill of the large form (the L=0 block's band holding n1 =
+    400..400+m, a few GB of CSR, above L2): the small case for ncu captures of
+    k_csr_fill in band mode."""
     import torch
     pkg = _pkg()
-    w = WORKLOAD
+    w = LARGE
     prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
     t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
-    L, par, spin, cf = workload_blocks(pkg, w)[args.profile_block]
+    L, M, par, spin, cf = block_list(pkg, w)[args.profile_band]
     with pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec) as h:
         h.slater()
         h.rk()
         h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
                    copy_out=False)
-        ch, cs = h.block_count(cf, L, w["full"], spin)
+        a, m = 400, 2
+        r, nh, ns = h.band_count(cf, L, a, m, True, spin)
+        dev = torch.device("cuda", 0)
+        mk = lambda n, dt: torch.empty(max(int(n), 1), dtype=dt, device=dev)
+        H = dict(index_ptr=mk(r + 1, torch.int64), indices=mk(nh, torch.int64),
+                 data=mk(nh, torch.complex128))
+        S = dict(index_ptr=mk(r + 1, torch.int64), indices=mk(ns, torch.int64),
+                 data=mk(ns, torch.complex128))
+        torch.cuda.synchronize()
+        h.band_into(cf, L, a, m, True, spin, {x: v.data_ptr() for x, v in H.items()},
+                    {x: v.data_ptr() for x, v in S.items()})
+        h.synchronize()
+        tiles = np.unique(cf["n1"][(cf["n1"] >= a) & (cf["n1"] < a + m)].astype(np.int64) * 1000 +
+                          cf["n2"][(cf["n1"] >= a) & (cf["n1"] < a + m)]).size
+        print(json.dumps({"profile_band": args.profile_band, "L": L, "n1": [a, a + m - 1],
+                          "rows": int(r), "nnz_H": nh, "nnz_S": ns,
+                          "algorithmic_bytes": 24 * (nh + ns) + 16 * (r + 1) +
+                          8 * tile_doubles(w) * tiles, "tiles": int(tiles)}))
+
+
+def profile_block(args):
+    """Small case for ncu: one radial pass, then count + fill of one block of
+    the medium size into device buffers (block 0: 117,620 rows, ~2.9 GB)."""
+    import torch
+    pkg = _pkg()
+    w = MEDIUM
+    prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    L, M, par, spin, cf = block_list(pkg, w)[args.profile_block]
+    with pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec) as h:
+        h.slater()
+        h.rk()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+        ch, cs = h.block_count(cf, L, True, spin)
         n = cf.size
         dev = torch.device("cuda", 0)
-        Hd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
-                  indices=torch.empty(ch, dtype=torch.int64, device=dev),
-                  data=torch.empty(ch, dtype=torch.complex128, device=dev))
-        Sd = dict(index_ptr=torch.empty(n + 1, dtype=torch.int64, device=dev),
-                  indices=torch.empty(cs, dtype=torch.int64, device=dev),
-                  data=torch.empty(cs, dtype=torch.complex128, device=dev))
+        mk = lambda m, dt: torch.empty(max(int(m), 1), dtype=dt, device=dev)
+        Hd = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(ch, torch.int64),
+                  data=mk(ch, torch.complex128))
+        Sd = dict(index_ptr=mk(n + 1, torch.int64), indices=mk(cs, torch.int64),
+                  data=mk(cs, torch.complex128))
         torch.cuda.synchronize()
-        h.block_fill_into(cf, L, w["full"], spin, {x: v.data_ptr() for x, v in Hd.items()},
+        h.block_fill_into(cf, L, True, spin, {x: v.data_ptr() for x, v in Hd.items()},
                           {x: v.data_ptr() for x, v in Sd.items()}, on_device=True)
         h.synchronize()
         print(json.dumps({"profile_block": args.profile_block, "L": L, "spin": spin,
@@ -505,169 +1070,17 @@ def run_batch(args):
     }
 
 
-LARGE = dict(k=9, n_b=800, r_max=800.0, q=12, max_k=20, l_max=10, max_L=5, Z=2, cap_order=2,
-               cap_r0=10.0, cap_eta=1e-3)
-
-
-def run_large(args, sample_rows=2048):
-    """The large configuration (order 9, N=800, r_max=800, 12 GL points,
-    k=0..20, l_max=10, singlet L=0..5 with the L+-1 dipole blocks, q=0).  Its
-    CSR (terabytes) exceeds HBM and host memory, so: the radial stage and the
-    exact non-zero counts of every block are measured in full; H/S assembly
-    and dipole blocks are timed on row samples (3 ranges per block) and the
-    full-block time is extrapolated from the sample rate; the mixed path is
-    compared with the FP64 path on the same samples."""
-    import torch
-    pkg = _pkg()
-    w = LARGE
-    dev = torch.device("cuda", 0)
-    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
-    syms = pkg.basis.symmetries(w["max_L"], True)
-    cfs = [(L, M, par, pkg.configs(L, par, w["l_max"], w["n_b"], w["k"])) for (L, M, par) in syms]
-    out = {"metric": "large configuration: R^k stage, counts, sampled assembly", "config": {
-        "workload": "k=9 N=800 r_max=800 q=12 k=0..20 l_max=10 singlet L=0..5 + dipole L+-1 (q=0)",
-        "rows": [int(cf.size) for (_, _, _, cf) in cfs], "sample_rows_per_range": sample_rows},
-        "data": "synthetic (deterministic knot grid, no dataset)"}
-    P = band_pairs(w["k"], w["n_b"])
-    elems = P * P * (w["max_k"] + 1)
-    hs = {}
-    for name, prec in (("fp64", pkg.PREC_FP64), ("mixed", pkg.PREC_MIXED)):
-        h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec)
-        stream = torch.cuda.ExternalStream(h.stream, device=dev)
-
-        def radial():
-            h.slater()
-            h.rk()
-            h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
-                       copy_out=False)
-        radial()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        radial()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        out["radial_s_" + name] = e0.elapsed_time(e1) / 1e3
-        hs[name] = (h, stream)
-    out["rk_elements"] = elems
-    out["rk_elements_per_s_fp64"] = elems / out["radial_s_fp64"]
-    out["rk_store_bytes"] = int(w["n_b"] ** 2 * (((w["max_k"] + 1) * (2 * w["k"] - 1) ** 2 + 1) // 2 * 2) * 8)
-    blocks = []
-    tot_s = {"fp64": 0.0, "mixed": 0.0}
-    worst = 0.0
-    worst_max = 0.0
-    for (L, M, par, cf) in cfs:
-        n = cf.size
-        b = {"L": L, "rows": int(n)}
-        t0 = time.perf_counter()
-        nH, nS = hs["fp64"][0].block_count(cf, L, True, 0)
-        b["count_s"] = time.perf_counter() - t0
-        b["nnz_H"], b["nnz_S"] = int(nH), int(nS)
-        b["csr_bytes"] = 24 * (nH + nS) + 16 * (n + 1)
-        samples = {}
-        for name in ("fp64", "mixed"):
-            h, stream = hs[name]
-            h.block_count(cf, L, True, 0)
-            ent, ms = 0, 0.0
-            vals = []
-            for frac in (0.05, 0.5, 0.9):
-                r0 = int(frac * n)
-                cnt = min(sample_rows, n - r0)
-                sh, ss = h.block_count_rows(cf, L, r0, cnt, True, 0)
-                bufs = [torch.empty(cnt + 1, dtype=torch.int64, device=dev),
-                        torch.empty(sh, dtype=torch.int64, device=dev),
-                        torch.empty(sh, dtype=torch.complex128, device=dev),
-                        torch.empty(cnt + 1, dtype=torch.int64, device=dev),
-                        torch.empty(ss, dtype=torch.int64, device=dev),
-                        torch.empty(ss, dtype=torch.complex128, device=dev)]
-                Hd = dict(index_ptr=bufs[0].data_ptr(), indices=bufs[1].data_ptr(),
-                          data=bufs[2].data_ptr())
-                Sd = dict(index_ptr=bufs[3].data_ptr(), indices=bufs[4].data_ptr(),
-                          data=bufs[5].data_ptr())
-                h.block_rows_into(cf, L, r0, cnt, True, 0, Hd, Sd)  # warm
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                torch.cuda.synchronize()
-                e0.record(stream)
-                h.block_rows_into(cf, L, r0, cnt, True, 0, Hd, Sd)
-                e1.record(stream)
-                torch.cuda.synchronize()
-                ms += e0.elapsed_time(e1)
-                ent += sh + ss
-                vals.append((bufs[1].cpu(), bufs[2].cpu(), bufs[4].cpu(), bufs[5].cpu()))
-                del bufs
-            rate = ent / (ms / 1e3)
-            samples[name] = vals
-            b["sample_entries_per_s_" + name] = rate
-            b["assembly_s_extrapolated_" + name] = (nH + nS) / rate
-            tot_s[name] += (nH + nS) / rate
-        same = True
-        rel = 0.0  # |mixed - fp64| / |fp64| over entries >= 1e-10 of the sample's largest
-        rel_max = 0.0  # |mixed - fp64| / largest |fp64| of the sample range
-        for (i1, d1, si1, sd1), (i2, d2, si2, sd2) in zip(samples["fp64"], samples["mixed"]):
-            same = same and torch.equal(i1, i2) and torch.equal(si1, si2)
-            for x, y in ((d1, d2), (sd1, sd2)):
-                ax = x.abs()
-                if ax.numel() == 0:
-                    continue
-                top = float(ax.max())
-                mask = ax >= 1e-10 * top
-                if mask.any():
-                    rel = max(rel, float(((y - x).abs()[mask] / ax[mask]).max()))
-                if top > 0:
-                    rel_max = max(rel_max, float((y - x).abs().max()) / top)
-        b["pattern_identical_mixed_vs_fp64"] = bool(same)
-        b["max_err_rel_to_entry_mixed_vs_fp64"] = rel
-        b["max_err_rel_to_sample_max_mixed_vs_fp64"] = rel_max
-        worst = max(worst, rel)
-        worst_max = max(worst_max, rel_max)
-        blocks.append(b)
-        torch.cuda.empty_cache()
-    out["blocks"] = blocks
-    out["assembly_s_extrapolated_fp64"] = tot_s["fp64"]
-    out["assembly_s_extrapolated_mixed"] = tot_s["mixed"]
-    # Relative to the entry, a value that cancels between the multipole terms
-    # shows the terms' rounding magnified; the 1e-9 bar is relative to the
-    # term magnitude, which tests/test_precision_report.py checks against the
-    # oracle on these blocks.
-    out["max_err_rel_to_entry_mixed_vs_fp64"] = worst
-    out["max_err_rel_to_sample_max_mixed_vs_fp64"] = worst_max
-    # dipole blocks L -> L+1, q = 0 (z polarisation), length gauge
-    h = hs["fp64"][0]
-    h.radial_dipole(0, copy_out=False)
-    dips = []
-    for (L1, M1, p1, cf1), (L2, M2, p2, cf2) in zip(cfs[:-1], cfs[1:]):
-        t0 = time.perf_counter()
-        nd = h.dip_block_count(cf1, (L1, M1, p1), cf2, (L2, M2, p2), 0)
-        tc = time.perf_counter() - t0
-        r0 = cf1.size // 2
-        rows = cf1[r0:r0 + sample_rows]
-        h.dip_block(rows, (L1, M1, p1), cf2, (L2, M2, p2), 0)  # warm
-        t0 = time.perf_counter()
-        D = h.dip_block(rows, (L1, M1, p1), cf2, (L2, M2, p2), 0)
-        ts = time.perf_counter() - t0
-        rate = D["nnz"] / ts if ts > 0 else None
-        dips.append({"L": [L1, L2], "nnz": int(nd), "count_s": tc, "sample_nnz": int(D["nnz"]),
-                     "sample_s_host_outputs": ts,
-                     "fill_s_extrapolated": (nd / rate) if rate else None})
-    out["dipole_blocks"] = dips
-    for (h, _) in hs.values():
-        h.close()
-    return out
-
-
 def run_matvec(args):
     """CSR_mv / CSR_mv_sym (bs2e_csr_mv on device pointers) over the H blocks of
-    the bench workload, assembled into HBM by the library: achieved GB/s of
-    the mat-vec kernel against the measured copy bandwidth."""
+    the medium size, assembled into HBM by the library: achieved GB/s of the
+    mat-vec kernel against the measured copy bandwidth."""
     import torch
     pkg = _pkg()
-    w = WORKLOAD
+    w = MEDIUM
     dev = torch.device("cuda", 0)
     prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
     t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
-    blocks = workload_blocks(pkg, w)
+    blocks = block_list(pkg, w)
     res = {}
     with pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec) as h:
         h.slater()
@@ -677,7 +1090,7 @@ def run_matvec(args):
         stream = torch.cuda.ExternalStream(h.stream, device=dev)
         for op, full, name in ((0, True, "csr_mv"), (2, False, "csr_mv_sym")):
             t_ms, nbytes, nnz_all, cplx_all = 0.0, 0, 0, 0.0
-            for (L, par, spin, cf) in blocks[:4]:
+            for (L, M, par, spin, cf) in blocks[:4]:
                 nH, nS = h.block_count(cf, L, full, spin)
                 n = cf.size
                 ptr = torch.empty(n + 1, dtype=torch.int64, device=dev)
@@ -709,8 +1122,6 @@ def run_matvec(args):
                 e1.record(stream)
                 torch.cuda.synchronize()
                 t_ms += e0.elapsed_time(e1) / args.steps
-                # algorithmic bytes: int64 column + complex128 value per entry,
-                # two row pointers per row, x read once and y written once
                 nbytes += 24 * nH + 8 * (n + 1) + 32 * n
                 nnz_all += nH
                 cplx_all = cplx_all + cplx * nH
@@ -723,9 +1134,20 @@ def run_matvec(args):
                          "achieved_gbs": gbs, "frac_of_measured_hbm": gbs / peak,
                          "peak_source": src}
     return {"metric": "H x: CSR mat-vec over the L=0..3 singlet H blocks", "results": res,
-            "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 singlet",
-                       "precision_of_blocks": args.precision},
+            "config": {"workload": "order 7, N=200, r_max=200, q=10, k=0..10, l_max=5, "
+                                   "L=0..3 singlet", "precision_of_blocks": args.precision},
             "steps": args.steps, "warmup": args.warmup}
+
+
+# --------------------------------------------------------------------------
+# ranks
+# --------------------------------------------------------------------------
+def _barrier(world):
+    import torch
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
 
 
 def _max_over_ranks(x, world):
@@ -738,26 +1160,44 @@ def _max_over_ranks(x, world):
     return float(t.item())
 
 
+def _sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
 def run_reference(args):
-    """The reference's algorithm on the host cores (the oracle port), same metric."""
+    """The reference's algorithm on the host cores (the oracle port, all host
+    threads), same workload, metric and unit: each step is the CPU sample of
+    the job described in CpuSample; ms_per_step is the measured time of that
+    sample and value the sample's fraction of the job's R^k elements per
+    second of it."""
     pkg = _pkg()
-    w = WORKLOAD
-    for _ in range(args.warmup):
-        cpu_baseline(pkg, w, rows_per_block=8)
-    vals = []
+    w = WORKLOADS[args.workload]
+    cs = CpuSample(pkg, w)
+    for i in range(args.warmup):
+        cs.run(w["cpu_frac"] / 8, seed=100 + i)
+    vals, ts = [], []
     last = None
-    for _ in range(args.steps):
-        last = cpu_baseline(pkg, w)
+    for i in range(args.steps):
+        last = cs.run(w["cpu_frac"], seed=1 + i)
         vals.append(last["value"])
-    v = statistics.median(vals)
+        ts.append(last["t_s"])
+    v = sum(w["cpu_frac"] * rk_elements(w) for _ in ts) / sum(ts)
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "R^k elements/s",
         "n_gpus": args.gpus, "gpus_used": 0,  # the run's N; the arm itself runs on host cores
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * last["t_full_s"],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(ts),
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (deterministic knot grid, no dataset)",
-        "config": {"workload": "k=7 N=200 r_max=200 q=10 k=0..10 l_max=5 L=0..3 "
-                               "singlet+triplet full blocks (8 blocks)"},
+        "config": {"workload": workload_string(w),
+                   "step": "the oracle on fraction f=%.3g of every stage of one job" %
+                           w["cpu_frac"]},
+        "full_job_s_extrapolated": statistics.mean(ts) / w["cpu_frac"],
         "cpu_baseline": {"value": v, "unit": "R^k elements/s", "cores": last["cores"],
                          "kind": "port", "sample": last["sample"]},
         "e2e": {"value": v, "unit": "R^k elements/s", "h2d_bytes_per_step": 0,
@@ -768,27 +1208,30 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--profile-block", type=int, default=None)
-    ap.add_argument("--workload", default="order7_n200",
-                    choices=["order7_n200", "batch", "matvec", "order9_n800"])
+    ap.add_argument("--profile-band", type=int, default=None)
+    ap.add_argument("--workload", default="order9_n800",
+                    choices=["order9_n800", "order7_n200", "batch", "matvec"])
     args = ap.parse_args()
     if args.profile_block is not None:
         profile_block(args)
+        return
+    if args.profile_band is not None:
+        profile_band(args)
         return
     if args.workload == "batch":
         print(json.dumps(run_batch(args)), flush=True)
         return
     if args.workload == "matvec":
         print(json.dumps(run_matvec(args)), flush=True)
-        return
-    if args.workload == "order9_n800":
-        print(json.dumps(run_large(args)), flush=True)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -801,7 +1244,8 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
-    res = run_ours(args, rank, world)
+    res = run_large(args, rank, world) if args.workload == "order9_n800" else \
+        run_medium(args, rank, world)
     if rank == 0:
         print(json.dumps(res), flush=True)
     if world > 1:

@@ -325,11 +325,14 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
  * per_n1 != NULL, per n1 of the range the triple (rows, nnz_H, nnz_S) in
  * per_n1[3*i .. 3*i+2] (for choosing bands that fit a buffer).  fill_band
  * writes the band's CSR (range-local 1-based index_ptr, n_rows + 1 entries;
- * the block's 1-based column indices) into DEVICE arrays on the handle's
- * device, and, when rows != NULL (device, n_rows entries), the 1-based block
- * row of every band row.  The same configuration list, L, spin and full as
- * bs2e_block_count_ex.  No counterpart in the reference (its blocks are built
- * whole, hamiltonian.f90:106-283). */
+ * the block's 1-based column indices) and, when rows != NULL (n_rows
+ * entries), the 1-based block row of every band row.  out_on_device = 1: the
+ * seven arrays are device arrays on the handle's device; 0: host arrays, the
+ * band assembled in one of the handle's HBM staging areas
+ * (bs2e_opts.stage_bytes) and copied out, so the band must fit one area
+ * (BS2E_ERR_ARG otherwise: choose a narrower band).  The same configuration
+ * list, L, spin and full as bs2e_block_count_ex.  No counterpart in the
+ * reference (its blocks are built whole, hamiltonian.f90:106-283). */
 BS2E_API bs2e_status bs2e_block_band_count(bs2e_handle *h, const bs2e_config *configs,
                                            int64_t n_config, int64_t L, int64_t spin,
                                            int64_t full, int64_t n1_first, int64_t n1_count,
@@ -341,7 +344,7 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
                                           int64_t *rows, int64_t *H_index_ptr,
                                           int64_t *H_indices, double *H_data,
                                           int64_t *S_index_ptr, int64_t *S_indices,
-                                          double *S_data);
+                                          double *S_data, int64_t out_on_device);
 
 /* Host-side planning of band work (no device, no handle; safe to call from
  * any thread or rank).  Multi-GPU assembly hands each rank whole bands: the

@@ -70,6 +70,12 @@ def test_bands_equal_block_rows(bs2e, oracle, precision):
                     w = _rows_of(full, want)
                     for x in ("index_ptr", "indices", "data"):
                         np.testing.assert_array_equal(got[x], w[x])
+                if (a, m) == (5, 9):  # the same band into host arrays
+                    rows_h, Hh, Sh = h.band(cf, L, a, m, True, spin)
+                    np.testing.assert_array_equal(rows_h, rows)
+                    for got, dv in ((Hh, H), (Sh, S)):
+                        for x in ("index_ptr", "indices", "data"):
+                            np.testing.assert_array_equal(got[x], dv[x])
             # the whole block (which the bands reproduce) against the oracle
             Hr, Sr = oracle.construct_block(cf, L, c["k"], N, c["max_k"], ref["R"], ref["H1p"],
                                             ref["S"], True, spin)
@@ -91,9 +97,25 @@ def test_block_cache_off_recounts(bs2e):
         off = [h.block_count(cf, L, True, spin) for (L, M, par, spin, cf) in bl]
         recount = h.launch_count - n0
         assert first == again == off
-        # a recount runs the planning and count kernels besides the compare
-        assert recount >= cached + 3 * (len(bl) - 1)
+        # kept blocks cost one compare kernel each; without the cache every
+        # block runs its channel-marks, segment-plan and count kernels again
+        assert cached == len(bl)
+        assert recount >= 3 * len(bl)
         with pytest.raises(bs2e.Bs2eError):
             h.set_block_cache(17)
         h.set_block_cache(16)
         assert [h.block_count(cf, L, True, spin) for (L, M, par, spin, cf) in bl] == first
+
+
+def test_host_band_larger_than_staging_is_refused(bs2e):
+    c = CASES["small2"]
+    with bs2e.Bs2e(knots(bs2e, "small2"), c["k"], c["q"], c["max_k"], stage_bytes=65536) as h:
+        h.slater()
+        h.rk()
+        h.one_body(c["Z"], c["lmax"] + 1)
+        L, M, par, spin, cf = blocks(bs2e, "small2")[0]
+        with pytest.raises(bs2e.Bs2eError) as e:
+            h.band(cf, L, 1, c["n_b"], True, spin)
+        assert e.value.status == 1 and "staging" in str(e.value)
+        rows, H, S = h.band(cf, L, 1, 1, True, spin)  # one n1 of the first channel fits
+        assert rows.size == int((cf["n1"] == 1).sum())

@@ -19,8 +19,10 @@ reference), on both the FP64 and the mixed path, through the C ABI:
 
 Bars: CSR patterns bit-exact; R^k elements within 1e-12 relative (both
 stores); H entries within 1e-12 of their term scale for the FP64 path and
-1e-11 for the mixed path, and per entry (entries >= 1e-15 Eh, see
-parity_util) within 1e-12 (FP64) and 1e-9 (mixed); S entries per entry
+1e-11 for the mixed path, and per entry within 1e-12 (FP64) and 1e-9
+(mixed) for entries of at least 1e-15 Eh whose terms do not cancel below
+1e-3 of their magnitudes (parity_util says why the others take the
+term-scale bar; their per-entry figure is reported); S entries per entry
 within 1e-12.  The one-body matrices of both sides are their own (GPU
 bs2e_one_body, oracle setup_H1p / setup_S).  With BS2E_REPORT_DIR set, every
 figure is written there as JSON.
