@@ -1011,8 +1011,11 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, con
     }
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(128, MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64) k_csr_fill(FillArgs F) {
+// BIG: the variant for R^k tiles too large for 8 CTAs per SM (above ~22 KB:
+// order 9 with k <= 20 stages 48.5 KB), compiled for 4 CTAs per SM so the
+// entry loops get up to 128 registers instead of spilling at 64.
+template <bool MIXED, bool BIG>
+__global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64)) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
     __shared__ int sexp[kMaxK1];
@@ -1265,13 +1268,17 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     }
     if (h->plan.n_config > 0 && r.row1 > r.row0 && r.a1 >= r.a0) {
         const unsigned tiles = (unsigned)((int64_t)(r.a1 - r.a0 + 1) * h->g.N);
-        if (h->precision == BS2E_PREC_MIXED) {
-            cudaFuncSetAttribute(k_csr_fill<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_csr_fill<true><<<tiles, 128, smem, h->stream>>>(F);
-        } else {
-            cudaFuncSetAttribute(k_csr_fill<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_csr_fill<false><<<tiles, 128, smem, h->stream>>>(F);
-        }
+        // 8 CTAs of 128 threads fit an SM while each stages at most ~22 KB
+        const bool big = smem > (size_t)22 * 1024;
+        auto go = [&](auto kern) {
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<tiles, 128, smem, h->stream>>>(F);
+        };
+        const bool mixed = h->precision == BS2E_PREC_MIXED;
+        if (mixed && big) go(k_csr_fill<true, true>);
+        else if (mixed) go(k_csr_fill<true, false>);
+        else if (big) go(k_csr_fill<false, true>);
+        else go(k_csr_fill<false, false>);
         h->launches++;
     }
 }

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 
+#include "bs2e_dmul.h"
 #include "bs2e_internal.h"
 
 namespace bs2e {
@@ -264,23 +265,42 @@ __device__ void rk_near_stage(const RadialDev &P, int a, int b, int kk, double *
     const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
     const int base2 = b - k + 2;
     const double *__restrict__ mom = P.mom;
-    for (int x = threadIdx.x; x < 2 * W * k; x += blockDim.x) {
-        const bool ac = x < W * k;
-        const int y = ac ? x : x - W * k;
-        const int off = y / k, j = y - off * k;
+    // (a, c) part: one thread per offset walks Pm forward and SM backward as
+    // running sums of the moments (additions of positive terms only);
+    // (b, d) part: one thread per (offset, j)
+    for (int x = threadIdx.x; x < W + W * k; x += blockDim.x) {
+        const bool ac = x < W;
+        const int y = ac ? x : x - W;
+        const int off = ac ? y : y / k, j = ac ? 0 : y - off * k;
         const int iv2 = base2 + j;
         double v0 = 0.0, v1 = 0.0;
         if (ac) {
             const int c = a + off - (k - 1);
             if (c >= 0 && c < N) {
                 const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-                for (int iv1 = lop; iv1 <= min(hip, iv2 - 1); ++iv1)
-                    v0 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
-                for (int iv1 = max(lop, iv2 + 1); iv1 <= hip; ++iv1)
-                    v1 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+                const double *m0 = mom + (size_t)kk * 2 * k2 + (a + 1) * k + (c + 1);
+                // moment of interval iv1: m0[iv1 * (K1 2 k^2 - k - 1)] (+ k^2 for M)
+                const size_t st = (size_t)K1 * 2 * k2 - (size_t)(k + 1);
+                double pm = 0.0;  // sum over iv1 < iv2_j
+                for (int iv1 = lop; iv1 <= min(hip, base2 - 1); ++iv1) pm += m0[iv1 * st];
+                for (int jj = 0; jj < k; ++jj) {
+                    s[jj * W + off] = pm;  // Pm
+                    const int iv = base2 + jj;
+                    if (iv >= lop && iv <= hip) pm += m0[iv * st];
+                }
+                double sm = 0.0;  // sum over iv1 > iv2_j
+                for (int iv1 = hip; iv1 >= max(lop, base2 + k); --iv1) sm += m0[iv1 * st + k2];
+                for (int jj = k - 1; jj >= 0; --jj) {
+                    s[(k + jj) * W + off] = sm;  // SM
+                    const int iv = base2 + jj;
+                    if (iv >= lop && iv <= hip) sm += m0[iv * st + k2];
+                }
+            } else {
+                for (int jj = 0; jj < k; ++jj) {
+                    s[jj * W + off] = 0.0;
+                    s[(k + jj) * W + off] = 0.0;
+                }
             }
-            s[j * W + off] = v0;          // Pm
-            s[(k + j) * W + off] = v1;    // SM
         } else {
             const int d = b + off - (k - 1);
             if (d >= 0 && d < N) {
@@ -347,10 +367,12 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
             if (c < 0 || c >= N || d < 0 || d >= N) {
                 for (int kk = k_first; kk < k_first + k_count; ++kk) o[kk * W2] = 0.0;
             } else {
+                // one product per element, on the integer pipes (bit for bit
+                // the FP64 multiply; bs2e_dmul.h says why)
                 const double *x1 = P.tot + lower + (size_t)a * W + dc;
                 const double *x2 = P.tot + upper + (size_t)b * W + dd;
                 for (int kk = k_first; kk < k_first + k_count; ++kk)
-                    o[kk * W2] = x1[kk * NW] * x2[kk * NW];
+                    o[kk * W2] = dmul_int(x1[kk * NW], x2[kk * NW]);
             }
             dc += step_dc;
             dd += step_dd;
