@@ -480,19 +480,6 @@ class LargeJob:
         with self.torch.cuda.stream(self.stream):
             self.ysum += self.y[:r].sum()
 
-    def band_sample(self, u):
-        """Device copy of one band's H data (for precision comparisons)."""
-        torch, h = self.torch, self.h
-        L, M, par, spin, cf = self.blocks[u["block"]]
-        r, nH, nS = u["rows"], u["nH"], u["nS"]
-        Hp, Hi, Hd, Sp, Si, Sd = self._layout([8 * (r + 1), 8 * nH, 16 * nH, 8 * (r + 1),
-                                               8 * nS, 16 * nS])
-        h.band_into(cf, L, u["n1"], u["m"], True, spin, dict(index_ptr=Hp, indices=Hi, data=Hd),
-                    dict(index_ptr=Sp, indices=Si, data=Sd))
-        off = (8 * (r + 1) + 255) // 256 * 256 + (8 * nH + 255) // 256 * 256
-        data = self.area.view(torch.uint8)[off:off + 16 * nH].view(torch.complex128)
-        return data.clone()
-
     def e2e_chunk(self, j, host):
         """Chunk j through the C ABI with host outputs (pinned buffers in host);
         returns (h2d bytes, d2h bytes)."""
@@ -623,13 +610,11 @@ def run_large(args, rank, world):
     }
     if res["radial_s"]:
         res["rk_stage_elements_per_s"] = elems / res["radial_s"]
-    # mixed vs FP64: the other precision over one whole job, and errors on sampled bands
+    cs = CpuSample(pkg, w) if rank == 0 and world == 1 else None
+    # mixed vs FP64: the other precision over one whole job, and the errors of
+    # both against the oracle on rows of every block
     if not args.no_mixed and world == 1:
         other = "mixed" if prec_main == "fp64" else "fp64"
-        samples = _sample_units(job)
-        ref = [job.band_sample(u) for u in samples]
-        job.close()
-        torch.cuda.empty_cache()
         job2 = LargeJob(pkg, w, precs[other], area, rank, world, plan=job.plan)
         job2.run_chunk(0)
         torch.cuda.synchronize()
@@ -640,70 +625,87 @@ def run_large(args, rank, world):
             job2.run_chunk(j)
         t1.record(job2.stream)
         torch.cuda.synchronize()
-        got = [job2.band_sample(u) for u in samples]
-        err = _compare(ref, got) if prec_main == "fp64" else _compare(got, ref)
         t_other = t0.elapsed_time(t1) / 1e3
         res["mixed_vs_fp64"] = {
             other + "_job_s": t_other, prec_main + "_job_s": job_s,
             "mixed_speedup_vs_fp64": ((job_s / t_other) if prec_main == "fp64" else
                                       (t_other / job_s)) if job_s else None,
-            "errors_mixed_vs_fp64": err,
-            "sampled_bands": [(u["block"], u["n1"], u["m"], u["nH"]) for u in samples]}
+            "errors": _precision_sample(pkg, w, job.blocks, {prec_main: job.h, other: job2.h},
+                                        cs)}
         job2.close()
         torch.cuda.empty_cache()
-        job = LargeJob(pkg, w, precs[prec_main], area, rank, world, plan=job.plan)
     if not args.no_e2e and world == 1:
         res["e2e"] = _e2e_large(job, args, elems, total_bytes)
     job.close()
     del area
     torch.cuda.empty_cache()
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cs = CpuSample(pkg, w).run(w["cpu_frac"], seed=1)
-        res["cpu_baseline"] = {k: v for k, v in cs.items()
+    if cs is not None and not args.no_cpu_baseline:
+        r = cs.run(w["cpu_frac"], seed=1)
+        res["cpu_baseline"] = {k: v for k, v in r.items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
     return res
 
 
-def _sample_units(job, nmax=6, max_bytes=2 << 30):
-    """Small bands, one per block where one exists."""
-    out = []
-    for b in range(len(job.blocks)):
-        cands = [u for u in job.plan["units"] if u["kind"] == "band" and u["block"] == b and
-                 u["bytes"] <= max_bytes]
-        if cands:
-            out.append(min(cands, key=lambda u: u["bytes"]))
-    return out[:nmax]
+FLOOR_EH = 1e-15  # entries below this (Hartree) take the term-scale measure only
+CANCEL = 1e-3      # |entry| / sum of |terms| below which an entry is a cancellation
 
 
-def _compare(fp64_list, mixed_list, floor=1e-15):
-    """Mixed vs FP64 on the same bands: per entry (entries >= floor Eh) and
-    relative to the band's largest |entry|."""
-    import torch
-    e_max = e_ms = m_max = 0.0
-    n = n_below = 0
-    for a, b in zip(fp64_list, mixed_list):
-        if a.numel() == 0:
-            continue
-        d = (b - a).abs()
-        aa = a.abs()
-        top = float(aa.max())
-        mask = aa >= floor
-        if mask.any():
-            r = d[mask] / aa[mask]
-            e_max = max(e_max, float(r.max()))
-            e_ms += float((r * r).sum())
-            n += int(mask.sum())
-        n_below += int((~mask).sum())
-        if top > 0:
-            m_max = max(m_max, float(d.max()) / top)
-        del d, aa, mask
-    torch.cuda.empty_cache()
-    return {"entry_max": e_max, "entry_rms": (e_ms / n) ** 0.5 if n else 0.0,
-            "entry_floor_eh": floor, "entries": n, "entries_below_floor": n_below,
-            "rel_to_band_max_max": m_max,
-            "note": "per entry over entries >= the floor; a cancelling entry (terms summing "
-                    "to far below their magnitudes) shows the terms' rounding magnified, "
-                    "see the oracle parity tests for the term-scale figures"}
+def _errors(got, ref, scale):
+    """Max / RMS of |got - ref| over the term scale, and per entry over the
+    entries >= FLOOR_EH whose terms do not cancel below CANCEL (those are
+    reported apart)."""
+    d = np.abs(got - ref)
+    a = np.abs(ref)
+    t = d / np.maximum(scale, 1e-300)
+    ok = (a >= FLOOR_EH) & (a >= CANCEL * scale)
+    canc = (a >= FLOOR_EH) & ~ok
+    e = d[ok] / a[ok]
+    return {"term_max": float(t.max()) if t.size else 0.0,
+            "term_rms": float(np.sqrt(np.mean(t * t))) if t.size else 0.0,
+            "entry_max": float(e.max()) if e.size else 0.0,
+            "entry_rms": float(np.sqrt(np.mean(e * e))) if e.size else 0.0,
+            "cancel_entry_max": float((d[canc] / a[canc]).max()) if canc.any() else 0.0,
+            "entries": int(t.size), "entries_cancelling": int(canc.sum()),
+            "entries_below_floor": int((a < FLOOR_EH).sum())}
+
+
+def _precision_sample(pkg, w, blocks, handles, cs, places=3, per=8):
+    """Rows of every block from each GPU path (handles: name -> Bs2e) and from
+    the oracle, which assembles them from R^k tiles it builds from the knots
+    (rk_tiles) and its own one-body matrices: each path against the oracle
+    at both normalisations, and mixed against FP64."""
+    from concurrent.futures import ThreadPoolExecutor
+    O = cs.O
+    jobs, need = [], set()
+    for (L, M, par, spin, cf) in blocks:
+        for r0 in np.linspace(0, cf.size - per, places).astype(np.int64):
+            jobs.append((L, spin, cf, int(r0)))
+            need |= set(zip(cf["n1"][r0:r0 + per].tolist(), cf["n2"][r0:r0 + per].tolist()))
+    need = np.array(sorted(need), dtype=np.int64)
+    T = O.rk_tiles(cs.t, w["k"], w["q"], w["max_k"], need, nthreads=cs.threads)
+    tab = O.tile_table(w["n_b"], need)
+
+    def oracle_rows(j):
+        L, spin, cf, r0 = j
+        return O.construct_block(cf, L, w["k"], w["n_b"], w["max_k"], T, cs.H1p, cs.S, True,
+                                 spin, rows=(r0, r0 + per), tile_of=tab)[0]
+
+    with ThreadPoolExecutor(max_workers=cs.threads) as ex:
+        ref = list(ex.map(oracle_rows, jobs))
+    got = {name: [h.block_rows(cf, L, r0, per, True, spin)[0] for (L, spin, cf, r0) in jobs]
+           for name, h in handles.items()}
+    for name in got:  # patterns bit-exact
+        for g, r in zip(got[name], ref):
+            assert np.array_equal(g["indices"], r["indices"]), name
+    cat = lambda xs, key: np.concatenate([x[key] for x in xs])
+    rd, sc = cat(ref, "data"), cat(ref, "scale")
+    out = {"rows": len(jobs) * per, "pattern": "bit-exact against the oracle",
+           "entry_floor_eh": FLOOR_EH, "cancel_below": CANCEL}
+    for name in got:
+        out[name + "_vs_oracle"] = _errors(cat(got[name], "data"), rd, sc)
+    if "fp64" in got and "mixed" in got:
+        out["mixed_vs_fp64"] = _errors(cat(got["mixed"], "data"), cat(got["fp64"], "data"), sc)
+    return out
 
 
 def _e2e_large(job, args, elems, total_bytes):
@@ -849,10 +851,9 @@ def run_medium(args, rank, world):
                      "launches_per_step": len(mine), "fill_s_per_step": sums.get("fill", 0) / args.steps},
         "clocks": clk.summary(),
     }
+    cs = CpuSample(pkg, w) if rank == 0 and world == 1 else None
     if not args.no_mixed and world == 1:
         other = "mixed" if args.precision == "fp64" else "fp64"
-        sel = [i for i in mine if blocks[i][0] == 0]
-        ref = {i: out_dev[i][0]["data"][:counts[i][0]].clone() for i in sel}
         h2 = make(other)
         for _ in range(2):
             step(h2, ptrs)
@@ -866,26 +867,22 @@ def run_medium(args, rank, world):
             step(h2, ptrs)
         a1.record(s2)
         torch.cuda.synchronize()
-        got = {i: out_dev[i][0]["data"][:counts[i][0]].clone() for i in sel}
-        pair = ([ref[i] for i in sel], [got[i] for i in sel])
-        err = _compare(*pair) if args.precision == "fp64" else _compare(pair[1], pair[0])
         t2 = a0.elapsed_time(a1) / 1e3 / n2
         res["mixed_vs_fp64"] = {other + "_ms_per_step": 1e3 * t2,
                                 args.precision + "_ms_per_step": 1e3 * t_dev / args.steps,
                                 "mixed_speedup_vs_fp64": (t_dev / args.steps / t2)
                                 if args.precision == "fp64" else (t2 / (t_dev / args.steps)),
-                                "errors_mixed_vs_fp64": err,
-                                "compared": "every H entry of the L=0 blocks"}
+                                "errors": _precision_sample(pkg, w, blocks,
+                                                            {args.precision: h, other: h2}, cs)}
         h2.close()
-        del ref, got
     if not args.no_e2e and world == 1:
         del out_dev
         torch.cuda.empty_cache()
         res["e2e"] = _e2e_medium(h, pkg, w, blocks, mine, counts, args, elems, t, radial)
     h.close()
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cs = CpuSample(pkg, w).run(w["cpu_frac"], seed=1)
-        res["cpu_baseline"] = {k: v for k, v in cs.items()
+    if cs is not None and not args.no_cpu_baseline:
+        r = cs.run(w["cpu_frac"], seed=1)
+        res["cpu_baseline"] = {k: v for k, v in r.items()
                                if k in ("value", "unit", "cores", "kind", "sample")}
     return res
 
@@ -932,12 +929,14 @@ def _e2e_medium(h, pkg, w, blocks, mine, counts, args, elems, t, radial):
 # small cases for ncu, the ragged batch and the mat-vec
 # --------------------------------------------------------------------------
 def profile_band(args):
-    """One band fill of the large form (the L=0 block's band holding n1 =
-    400..400+m, a few GB of CSR, above L2): the small case for ncu captures of
+    """One band fill of the large form's method (order 9, q=12, k=0..20,
+    l_max=10: 48.5 KB R^k tiles) on N = --profile-nb splines (r_max = N):
+    block --profile-band, n1 = N/2 and N/2+1, a few GB of CSR (above L2).
+    With N=200 the R^k store is 1.9 GB: the small case for ncu captures of
     k_csr_fill in band mode."""
     import torch
     pkg = _pkg()
-    w = LARGE
+    w = dict(LARGE, n_b=args.profile_nb, r_max=float(args.profile_nb))
     prec = pkg.PREC_MIXED if args.precision == "mixed" else pkg.PREC_FP64
     t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
     L, M, par, spin, cf = block_list(pkg, w)[args.profile_band]
@@ -946,7 +945,7 @@ def profile_band(args):
         h.rk()
         h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
                    copy_out=False)
-        a, m = 400, 2
+        a, m = w["n_b"] // 2, 2
         r, nh, ns = h.band_count(cf, L, a, m, True, spin)
         dev = torch.device("cuda", 0)
         mk = lambda n, dt: torch.empty(max(int(n), 1), dtype=dt, device=dev)
@@ -1218,6 +1217,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--profile-block", type=int, default=None)
     ap.add_argument("--profile-band", type=int, default=None)
+    ap.add_argument("--profile-nb", type=int, default=200)
     ap.add_argument("--workload", default="order9_n800",
                     choices=["order9_n800", "order7_n200", "batch", "matvec"])
     args = ap.parse_args()
