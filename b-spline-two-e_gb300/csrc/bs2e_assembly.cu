@@ -520,11 +520,87 @@ __device__ __forceinline__ double wide_sums(const float2 *R2, const int *sexp, c
     return (sup && supx) ? rd + rx : (sup ? rd : rx);
 }
 
+// The rest of one mixed-path H entry once its multipole sums are known: the
+// direct (fd, in the frame 2^Ed, present when hd) and exchange (fx, 2^Ex, hx)
+// sums are joined, the one-body terms H_1p_neq (mat_els.f90:697-715; od: the
+// l_eq term under sup, ox: the l_eq_ex term under sup_x) are added -- as
+// FP32 pairs when the bands allow it (ff_one_body), else in FP64 -- and the
+// entry is rounded once to a double.  Real S only.  The operations are those
+// of the one-entry loop of fill_row, in the same order.
+__device__ __forceinline__ double2 mixed_finish(
+    const FillArgs &F, FF fd, FF fx, bool hd, bool hx, int Ed, int Ex, bool od, bool ox,
+    int n_a, int n_b, int n_c, int n_d, long long sgn_bit, const float4 *HaA, const float4 *HbB,
+    const float4 *SA, const float4 *SB, const double2 *HaR, const double2 *HbR,
+    const double2 *SaR, const double2 *SbR) {
+    int Ev = 0;
+    FF v = ff_join(fd, Ed, hd, fx, Ex, hx, Ev);
+    bool has = hd || hx;
+    double re = 0.0, im = 0.0;
+    if (F.ff_one_body) {
+        FF hi_im{0.f, 0.f};
+        bool fb = false;
+        if (od || ox) {
+            FF hr{0.f, 0.f};
+            if (od) {
+                const int dc = n_c - n_a, dd = n_d - n_b;
+                float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                hr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r), ff_mul(make_float2(h2.x, h2.y), s2r));
+                hi_im = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r), ff_mul(make_float2(h2.z, h2.w), s2r));
+            }
+            if (ox) {
+                const int dc = n_d - n_a, dd = n_c - n_b;
+                float4 h1 = HaA[dc], s1 = SB[dd], h2 = HbB[dd], s2 = SA[dc];
+                float2 s1r = make_float2(s1.x, s1.y), s2r = make_float2(s2.x, s2.y);
+                const bool ng = sgn_bit != 0;
+                FF xr = ff_add(ff_mul(make_float2(h1.x, h1.y), s1r), ff_mul(make_float2(h2.x, h2.y), s2r));
+                FF xi = ff_add(ff_mul(make_float2(h1.z, h1.w), s1r), ff_mul(make_float2(h2.z, h2.w), s2r));
+                hr = ff_add(hr, ff_neg_if(xr, ng));
+                hi_im = ff_add(hi_im, ff_neg_if(xi, ng));
+            }
+            if (!has || kRkBias - Ev <= 124) {
+                v = ff_join(v, Ev, has, hr, kRkBias, true, Ev);
+                has = true;
+            } else {
+                fb = true;
+                re = ff_to_double(hr, 0);
+            }
+        }
+        if (has) {
+            const double t = ff_to_double(v, Ev - kRkBias);
+            re = fb ? re + t : t;
+        }
+        im = (od || ox) ? ff_to_double(hi_im, 0) : 0.0;
+    } else {
+        if (has) re = ff_to_double(v, Ev - kRkBias);
+        if (od) {
+            const int dc = n_c - n_a, dd = n_d - n_b;
+            const double2 h1 = HaR[dc], h2 = HbR[dd];
+            const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+            re = fma(h1.x, s1, re);
+            re = fma(h2.x, s2, re);
+            im = fma(h1.y, s1, im);
+            im = fma(h2.y, s2, im);
+        }
+        if (ox) {
+            const int dc = n_d - n_a, dd = n_c - n_b;
+            const double2 h1 = HaR[dc], h2 = HbR[dd];
+            const double s1 = flip_sign(SbR[dd].x, sgn_bit);
+            const double s2 = flip_sign(SaR[dc].x, sgn_bit);
+            re = fma(h1.x, s1, re);
+            re = fma(h2.x, s2, re);
+            im = fma(h1.y, s1, im);
+            im = fma(h2.y, s2, im);
+        }
+    }
+    return make_double2(re, im);
+}
+
 // One row of the block (warp-wide): row (n_a, n_b) of channel c_r, with the R^k
 // tile of (n_a, n_b) at sR (shared memory when staged, global otherwise), its
 // per-multipole exponents at sexp (mixed store) and the warp's scratch for the
 // scaled multipole weights.
-template <bool MIXED>
+template <bool MIXED, bool BIG>
 __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, const int c_r,
                                          const int n_a, const int n_b, const double *sR,
                                          const int *sexp, float2 (*sAw)[kMaxK1],
@@ -751,6 +827,87 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, con
                         if (liveB) {
                             F.Hidx[oH + eB] = (int64_t)jB + 1;
                             F.Hdat[oH + eB] = make_double2(reB, imB);
+                        }
+                    }
+                } else if (MIXED && BIG && F.s_real && !F.gated && !wide) {
+                    // mixed path with registers to spare (large-tile variant):
+                    // two entries per lane as in the FP64 loop above, so the
+                    // FP32-pair accumulations of the two entries form
+                    // independent chains; each entry is then finished exactly
+                    // as the one-entry loop below does
+                    for (int e0 = 0; e0 < tot; e0 += 64) {
+                        const int eA = e0 + lane, eB = eA + 32;
+                        int pA = 0, pB = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1) {
+                            const int vA = __shfl_sync(FULL, excl, pA + step);
+                            const int vB = __shfl_sync(FULL, excl, pB + step);
+                            if (vA <= eA) pA += step;
+                            if (vB <= eB) pB += step;
+                        }
+                        int ncA, ndA, jA, ncB, ndB, jB;
+                        {
+                            const int o = eA - __shfl_sync(FULL, excl, pA);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pA);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pA), s2 = __shfl_sync(FULL, hs.s2, pA);
+                            ncA = __shfl_sync(FULL, n_c, pA);
+                            ndA = o < l1 ? s1 + o : s2 + (o - l1);
+                            jA = __shfl_sync(FULL, base, pA) + (ndA - __shfl_sync(FULL, lo, pA));
+                        }
+                        {
+                            const int o = eB - __shfl_sync(FULL, excl, pB);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pB);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pB), s2 = __shfl_sync(FULL, hs.s2, pB);
+                            ncB = __shfl_sync(FULL, n_c, pB);
+                            ndB = o < l1 ? s1 + o : s2 + (o - l1);
+                            jB = __shfl_sync(FULL, base, pB) + (ndB - __shfl_sync(FULL, lo, pB));
+                        }
+                        const bool liveA = eA < tot, liveB = eB < tot;
+                        const bool supA = liveA && abs(n_a - ncA) < k && abs(n_b - ndA) < k;
+                        const bool supxA = liveA && abs(n_a - ndA) < k && abs(n_b - ncA) < k;
+                        const bool supB = liveB && abs(n_a - ncB) < k && abs(n_b - ndB) < k;
+                        const bool supxB = liveB && abs(n_a - ndB) < k && abs(n_b - ncB) < k;
+                        // without gated pairs a direct (exchange) sum exists exactly
+                        // where sup (sup_x) holds and the list is non-empty
+                        const bool hdA = supA && pi.nd > 0, hxA = supxA && pi.nx > 0;
+                        const bool hdB = supB && pi.nd > 0, hxB = supxB && pi.nx > 0;
+                        FF fdA{0.f, 0.f}, fdB{0.f, 0.f}, fxA{0.f, 0.f}, fxB{0.f, 0.f};
+                        if (hdA || hdB) {
+                            // an entry without the sum reads a valid element and drops it
+                            const int oA = hdA ? (ncA - n_a + k - 1) * W + (ndA - n_b + k - 1) : 0;
+                            const int oB = hdB ? (ncB - n_a + k - 1) * W + (ndB - n_b + k - 1) : 0;
+#pragma unroll 4
+                            for (int u = 0; u < pi.nd; ++u) {
+                                const int ko = sKow[0][u];
+                                const float2 w = sAw[0][u];
+                                ff_madd(fdA, w, sR2[ko + oA]);
+                                ff_madd(fdB, w, sR2[ko + oB]);
+                            }
+                        }
+                        if (hxA || hxB) {
+                            const int oA = hxA ? (ndA - n_a + k - 1) * W + (ncA - n_b + k - 1) : 0;
+                            const int oB = hxB ? (ndB - n_a + k - 1) * W + (ncB - n_b + k - 1) : 0;
+#pragma unroll 4
+                            for (int u = 0; u < pi.nx; ++u) {
+                                const int ko = sKow[1][u];
+                                const float2 w = sAw[1][u];
+                                ff_madd(fxA, w, sR2[ko + oA]);
+                                ff_madd(fxB, w, sR2[ko + oB]);
+                            }
+                        }
+                        if (liveA) {
+                            F.Hidx[oH + eA] = (int64_t)jA + 1;
+                            F.Hdat[oH + eA] = mixed_finish(F, fdA, fxA, hdA, hxA, Ed, Ex,
+                                                           leq && supA, leqx && supxA, n_a, n_b,
+                                                           ncA, ndA, sgn_bit, HaA, HbB, SA, SB,
+                                                           HaR, HbR, SaR, SbR);
+                        }
+                        if (liveB) {
+                            F.Hidx[oH + eB] = (int64_t)jB + 1;
+                            F.Hdat[oH + eB] = mixed_finish(F, fdB, fxB, hdB, hxB, Ed, Ex,
+                                                           leq && supB, leqx && supxB, n_a, n_b,
+                                                           ncB, ndB, sgn_bit, HaA, HbB, SA, SB,
+                                                           HaR, HbR, SaR, SbR);
                         }
                     }
                 } else {
@@ -1060,7 +1217,7 @@ __global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS :
     if (!stage_tile(src, sR, (uint32_t)(F.tile * sizeof(double)), &bar, F.err)) return;
     const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int rr = warp; rr < nrow; rr += nwarp)
-        fill_row<MIXED>(F, srow[rr], sch[rr], n_a, n_b, sR, sexp, sA[warp], sKo[warp]);
+        fill_row<MIXED, BIG>(F, srow[rr], sch[rr], n_a, n_b, sR, sexp, sA[warp], sKo[warp]);
 }
 
 // Row mode, for row ranges inside one or two channels, where a tile holds a
@@ -1085,7 +1242,7 @@ __global__ void __launch_bounds__(128, 6) k_csr_fill_rows(FillArgs F) {
         for (int i = lane; i < A.K1; i += 32) sexpw[warp][i] = F.Rexp[tix * A.K1 + i];
         __syncwarp();
     }
-    fill_row<MIXED>(F, (int)(row - F.ptr_row0), c_r, n_a, n_b, R, sexpw[warp], sA[warp],
+    fill_row<MIXED, false>(F, (int)(row - F.ptr_row0), c_r, n_a, n_b, R, sexpw[warp], sA[warp],
                     sKo[warp]);
 }
 
