@@ -9,9 +9,10 @@ whole path on the GPU: Slater primitives, the R^k store (3.84e9 elements,
 and the assembly of the 6 symmetry blocks (5.3e11 H and S entries) and the
 5 dipole blocks (~6e10 entries): ~14 TB of CSR, more than HBM and host memory
 together.  The CSR is therefore made in n1 bands (bs2e_block_fill_band) and
-dipole row slices of at most one staging area (24 GiB) and consumed on the
-device as it is made: the mat-vec bs2e_csr_mv applies every band of H and S
-and every slice of D to a fixed vector (the product a solver needs).
+dipole row slices of at most one staging area (24 GiB; two areas in turn)
+and consumed on the device as it is made: the mat-vec bs2e_csr_mv applies
+every band of H and S and every slice of D to a fixed vector (the product a
+solver needs), on a second handle's stream while the next band fills.
 
 A bench step is 1/16 of a job: the job's bands and slices cut into 16
 chunks of nearly equal CSR bytes, chunk 0 also running the radial stage, so
@@ -285,10 +286,10 @@ class CpuSample:
 # --------------------------------------------------------------------------
 class LargeJob:
     """The large form on one handle: planned bands and dipole slices, cut into
-    chunks; run_chunk(j) assembles chunk j into the staging area and applies
-    it to fixed vectors with the library's mat-vec."""
+    chunks; run_chunk(j) assembles chunk j into the two staging areas and
+    applies it to fixed vectors with the library's mat-vec."""
 
-    def __init__(self, pkg, w, prec, area, rank=0, world=1, plan=None):
+    def __init__(self, pkg, w, prec, areas, rank=0, world=1, plan=None):
         import torch
         self.torch = torch
         self.pkg, self.w = pkg, w
@@ -298,8 +299,11 @@ class LargeJob:
                           device=self.dev.index, stage_bytes=w["area_bytes"])
         self.h.set_block_cache(0)
         self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
-        self.area = area
-        self.base = area.data_ptr()
+        # the consumer: a second handle (any basis; it only runs the mat-vec on
+        # device pointers) whose stream works while the next band fills
+        self.hc = pkg.Bs2e(pkg.grids.explin_knots(4, 8, 10.0), 4, 4, 0, device=self.dev.index)
+        self.cstream = torch.cuda.ExternalStream(self.hc.stream, device=self.dev)
+        self.areas = areas
         self.blocks = [(L, M, par, spin, self._pin(cf)) for (L, M, par, spin, cf)
                        in block_list(pkg, w)]
         self.radial()
@@ -406,78 +410,114 @@ class LargeJob:
     def chunk_bytes(self, j):
         return sum(u["bytes"] for u in self.chunks[j])
 
-    def _layout(self, parts):
-        """Device addresses of consecutive arrays in the area (256-byte aligned)."""
+    def _layout(self, parts, a):
+        """Device addresses of consecutive arrays in area a (256-byte aligned)."""
+        area = self.areas[a]
         out, off = [], 0
         for nbytes in parts:
-            out.append(self.base + off)
+            out.append(area.data_ptr() + off)
             off += (int(nbytes) + 255) // 256 * 256
-        assert off <= self.area.numel() * self.area.element_size()
+        assert off <= area.numel() * area.element_size()
         return out
 
     def run_chunk(self, j, timers=None):
-        """Chunk j on the device; timers: dict of lists of (event, event) pairs."""
+        """Chunk j on the device; timers: dict of lists of (event, event) pairs.
+        Units fill the two areas in turn on the library's stream; a consumer
+        thread applies each filled unit on the consumer handle's stream while
+        the next unit fills; the call returns when both are done."""
+        import queue
+        import threading
         torch, h = self.torch, self.h
         ev = (lambda: torch.cuda.Event(enable_timing=True)) if timers is not None else None
 
-        def mark(name, e0):
-            if timers is not None:
-                e1 = ev()
-                e1.record(self.stream)
-                timers.setdefault(name, []).append((e0, e1))
-
-        def start():
+        def start(stream):
             if timers is None:
                 return None
             e = ev()
-            e.record(self.stream)
+            e.record(stream)
             return e
 
-        if j == 0:
-            e0 = start()
-            self.radial()
-            mark("radial", e0)
-        for u in self.chunks[j]:
-            if u["kind"] == "band":
-                L, M, par, spin, cf = self.blocks[u["block"]]
-                if u["count_first"]:
-                    e0 = start()
-                    h.block_count(cf, L, True, spin)
-                    mark("count", e0)
-                r, nH, nS = u["rows"], u["nH"], u["nS"]
-                Hp, Hi, Hd, Sp, Si, Sd = self._layout([8 * (r + 1), 8 * nH, 16 * nH,
-                                                       8 * (r + 1), 8 * nS, 16 * nS])
-                e0 = start()
-                h.band_into(cf, L, u["n1"], u["m"], True, spin,
-                            dict(index_ptr=Hp, indices=Hi, data=Hd),
-                            dict(index_ptr=Sp, indices=Si, data=Sd))
-                mark("fill", e0)
-                e0 = start()
-                x, y = self.x[u["block"]].data_ptr(), self.y.data_ptr()
-                h.csr_mv_device(0, r, cf.size, nH, Hp, Hi, Hd, x, y)
-                self._acc(r)
-                h.csr_mv_device(0, r, cf.size, nS, Sp, Si, Sd, x, y)
-                self._acc(r)
-                mark("consume", e0)
-            else:
-                L1, M1, p1, _, c1 = self.blocks[u["block"]]
-                L2, M2, p2, _, c2 = self.blocks[u["block2"]]
-                rows = c1[u["r0"]:u["r1"]]
-                e0 = start()
-                n = h.dip_block_count(rows, (L1, M1, p1), c2, (L2, M2, p2), 0)
-                assert n == u["nnz"]
-                Dp, Di, Dd = self._layout([8 * (u["rows"] + 1), 8 * n, 16 * n])
-                h.dip_block_into(rows, (L1, M1, p1), c2, (L2, M2, p2), 0,
-                                 dict(index_ptr=Dp, indices=Di, data=Dd))
-                mark("dipole", e0)
-                e0 = start()
-                h.csr_mv_device(0, u["rows"], c2.size, n, Dp, Di, Dd,
-                                self.x[u["block2"]].data_ptr(), self.y.data_ptr())
-                self._acc(u["rows"])
-                mark("consume", e0)
+        def mark(name, e0, stream):
+            if timers is not None:
+                e1 = ev()
+                e1.record(stream)
+                timers.setdefault(name, []).append((e0, e1))
+
+        q = queue.Queue()
+        free = [threading.Event(), threading.Event()]
+        for f in free:
+            f.set()
+        err = []
+
+        def consumer():
+            try:
+                while True:
+                    item = q.get()
+                    if item is None:
+                        return
+                    a, n_rows, n_cols, mats, x = item
+                    e0 = start(self.cstream)
+                    for (nnz, P, I, D) in mats:
+                        self.hc.csr_mv_device(0, n_rows, n_cols, nnz, P, I, D, x,
+                                              self.y.data_ptr())
+                        self._acc(n_rows)
+                    mark("consume", e0, self.cstream)
+                    free[a].set()
+            except BaseException as e:  # the producer re-raises it
+                err.append(e)
+                for f in free:
+                    f.set()
+
+        th = threading.Thread(target=consumer)
+        th.start()
+        try:
+            if j == 0:
+                e0 = start(self.stream)
+                self.radial()
+                mark("radial", e0, self.stream)
+            for i, u in enumerate(self.chunks[j]):
+                a = i % 2
+                free[a].wait()
+                if err:
+                    break
+                free[a].clear()
+                if u["kind"] == "band":
+                    L, M, par, spin, cf = self.blocks[u["block"]]
+                    if u["count_first"]:
+                        e0 = start(self.stream)
+                        h.block_count(cf, L, True, spin)
+                        mark("count", e0, self.stream)
+                    r, nH, nS = u["rows"], u["nH"], u["nS"]
+                    Hp, Hi, Hd, Sp, Si, Sd = self._layout([8 * (r + 1), 8 * nH, 16 * nH,
+                                                           8 * (r + 1), 8 * nS, 16 * nS], a)
+                    e0 = start(self.stream)
+                    h.band_into(cf, L, u["n1"], u["m"], True, spin,
+                                dict(index_ptr=Hp, indices=Hi, data=Hd),
+                                dict(index_ptr=Sp, indices=Si, data=Sd))
+                    mark("fill", e0, self.stream)
+                    q.put((a, r, cf.size, [(nH, Hp, Hi, Hd), (nS, Sp, Si, Sd)],
+                           self.x[u["block"]].data_ptr()))
+                else:
+                    L1, M1, p1, _, c1 = self.blocks[u["block"]]
+                    L2, M2, p2, _, c2 = self.blocks[u["block2"]]
+                    rows = c1[u["r0"]:u["r1"]]
+                    e0 = start(self.stream)
+                    n = h.dip_block_count(rows, (L1, M1, p1), c2, (L2, M2, p2), 0)
+                    assert n == u["nnz"]
+                    Dp, Di, Dd = self._layout([8 * (u["rows"] + 1), 8 * n, 16 * n], a)
+                    h.dip_block_into(rows, (L1, M1, p1), c2, (L2, M2, p2), 0,
+                                     dict(index_ptr=Dp, indices=Di, data=Dd))
+                    mark("dipole", e0, self.stream)
+                    q.put((a, u["rows"], c2.size, [(n, Dp, Di, Dd)],
+                           self.x[u["block2"]].data_ptr()))
+        finally:
+            q.put(None)
+            th.join()
+        if err:
+            raise err[0]
 
     def _acc(self, r):
-        with self.torch.cuda.stream(self.stream):
+        with self.torch.cuda.stream(self.cstream):
             self.ysum += self.y[:r].sum()
 
     def e2e_chunk(self, j, host):
@@ -519,6 +559,7 @@ class LargeJob:
 
     def close(self):
         self.h.close()
+        self.hc.close()
 
 
 def run_large(args, rank, world):
@@ -527,10 +568,11 @@ def run_large(args, rank, world):
     w = LARGE
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    area = torch.empty(w["area_bytes"] // 8, dtype=torch.float64, device=dev)
+    areas = [torch.empty(w["area_bytes"] // 8, dtype=torch.float64, device=dev)
+             for _ in range(2)]
     prec_main = args.precision
     precs = {"fp64": pkg.PREC_FP64, "mixed": pkg.PREC_MIXED}
-    job = LargeJob(pkg, w, precs[prec_main], area, rank, world)
+    job = LargeJob(pkg, w, precs[prec_main], areas, rank, world)
     nc = w["n_chunks"]
     elems = rk_elements(w)
     total_bytes = sum(u["bytes"] for u in job.plan["units"])
@@ -615,7 +657,7 @@ def run_large(args, rank, world):
     # both against the oracle on rows of every block
     if not args.no_mixed and world == 1:
         other = "mixed" if prec_main == "fp64" else "fp64"
-        job2 = LargeJob(pkg, w, precs[other], area, rank, world, plan=job.plan)
+        job2 = LargeJob(pkg, w, precs[other], areas, rank, world, plan=job.plan)
         job2.run_chunk(0)
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
@@ -637,7 +679,7 @@ def run_large(args, rank, world):
     if not args.no_e2e and world == 1:
         res["e2e"] = _e2e_large(job, args, elems, total_bytes)
     job.close()
-    del area
+    del areas
     torch.cuda.empty_cache()
     if cs is not None and not args.no_cpu_baseline:
         r = cs.run(w["cpu_frac"], seed=1)
