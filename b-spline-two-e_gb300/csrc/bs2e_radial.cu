@@ -418,10 +418,13 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int kk = k_first + warp; kk < k_first + k_count; kk += nwarp) {
-        double m = 0.0;
-        for (int i = lane; i < W2; i += 32) m = fmax(m, sv[kk * W2 + i]);
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        int ex = (m > 0.0) ? ilogb(m) : 0;
+        // the slice maximum through the bit patterns (non-negative doubles
+        // order as unsigned integers), off the FP64 pipe
+        unsigned long long m = 0ull;
+        for (int i = lane; i < W2; i += 32)
+            m = max(m, (unsigned long long)__double_as_longlong(sv[kk * W2 + i]));
+        for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        int ex = m ? (int)(m >> 52) - 1023 : 0;  // ilogb of the (normal) maximum
         if (lane == 0) {
             sexp[kk] = ex;
             P.Rexp[(size_t)t * K1 + kk] = ex;
@@ -431,12 +434,13 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
     float2 *dst = P.Rf + (size_t)t * P.tile;
     for (int e = nel + threadIdx.x; e < P.tile; e += blockDim.x) dst[e] = make_float2(0.f, 0.f);
     for (int kk = k_first; kk < k_first + k_count; ++kk) {
-        const double scale = __longlong_as_double((long long)(1023 + kRkBias - sexp[kk]) << 52);
+        const int s = kRkBias - sexp[kk];
         for (int r = threadIdx.x; r < W2; r += blockDim.x) {
             const int e = kk * W2 + r;
-            double x = sv[e] * scale;
-            float hi = __double2float_rn(x);
-            float lo = __double2float_rn(x - (double)hi);
+            // (hi, lo) of sv[e] 2^s as the FP64 conversions give them, formed on
+            // the integer pipes (bs2e_dmul.h)
+            float hi, lo;
+            split_scaled(sv[e], s, hi, lo);
             dst[e] = make_float2(hi, lo);
         }
     }

@@ -53,6 +53,38 @@ int main(int argc, char **argv) {
                           -0.0, 1.0 / 0.0};
     for (double x : odd)
         for (double y : odd) check(x, y);
+    // split_scaled against the FP64 conversions it replaces
+    long sbad = 0, schecked = 0;
+    auto fb = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return u;
+    };
+    auto check_split = [&](double v, int s) {
+        volatile double vv = v;
+        const double x = vv * make((uint64_t)(1023 + s), 0);
+        const float hi_w = (float)x, lo_w = (float)(x - (double)hi_w);
+        float hi, lo;
+        bs2e::split_scaled(v, s, hi, lo);
+        ++schecked;
+        if (fb(hi) != fb(hi_w) || fb(lo) != fb(lo_w)) {
+            if (sbad < 10)
+                std::printf("split mismatch: v=%a s=%d want (%a, %a) got (%a, %a)\n", v, s,
+                            (double)hi_w, (double)lo_w, (double)hi, (double)lo);
+            ++sbad;
+        }
+    };
+    for (long i = 0; i < n / 2; ++i) {
+        const int s = (int)(rng() % 401) - 200;
+        check_split(make(1023 + (int64_t)(rng() % 401) - 200, rng()), s);
+        // few-bit significands: dropped parts exactly half, zero remainders
+        check_split(make(1023 + (int64_t)(rng() % 301) - 150, rng() & (0xFFFFFull << (rng() % 33))), s);
+        // far below the scale: hi and lo near or below the float normal range
+        check_split(make(1023 - 120 - (int64_t)(rng() % 40), rng()), 0);
+    }
+    check_split(0.0, 17);
+    check_split(1e-320, 50);
     std::printf("%ld products checked, %ld mismatches\n", checked, bad);
-    return bad ? 1 : 0;
+    std::printf("%ld splits checked, %ld mismatches\n", schecked, sbad);
+    return (bad || sbad) ? 1 : 0;
 }

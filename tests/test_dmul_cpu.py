@@ -1,8 +1,12 @@
-"""The integer double product of the R^k store (csrc/bs2e_dmul.h) equals the
-IEEE 754 multiply bit for bit: compiled for the host with g++ and checked on
-40 million products (random significands over the whole normal exponent
-range, few-bit significands whose products fall exactly halfway between two
-doubles, and the inputs that fall back to the FP64 multiply)."""
+"""The integer forms of the R^k store (csrc/bs2e_dmul.h) equal the FP64
+operations they replace, bit for bit: compiled for the host with g++, the
+product is checked against the IEEE 754 multiply on 40 million products
+(random significands over the whole normal exponent range, few-bit
+significands whose products fall exactly halfway between two doubles, and
+the inputs that fall back to the FP64 multiply), and the FP32-pair split of
+the mixed store against its FP64 conversions on 30 million values (random,
+few-bit and far below the scale, where the low word leaves the normal float
+range)."""
 import os
 import subprocess
 
