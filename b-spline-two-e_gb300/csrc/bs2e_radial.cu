@@ -265,43 +265,53 @@ __device__ void rk_near_stage(const RadialDev &P, int a, int b, int kk, double *
     const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
     const int base2 = b - k + 2;
     const double *__restrict__ mom = P.mom;
-    // (a, c) part: one thread per offset walks Pm forward and SM backward as
-    // running sums of the moments (additions of positive terms only);
+    // (a, c) part: one warp per offset; lane j takes the moments of interval
+    // iv2_j, lanes also take the head (iv1 < iv2_0) and tail (iv1 > iv2_{k-1})
+    // terms, and shuffle scans give Pm (exclusive prefix) and SM (exclusive
+    // suffix); all additions are of positive terms
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const size_t st = (size_t)K1 * 2 * k2 - (size_t)(k + 1);  // interval stride of mom
+    for (int off = warp; off < W; off += nwarp) {
+        const int c = a + off - (k - 1);
+        double pm = 0.0, sm = 0.0;
+        if (c >= 0 && c < N) {  // warp-uniform
+            const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
+            // moment of interval iv1: m0[iv1 * st] (+ k^2 for M)
+            const double *m0 = mom + (size_t)kk * 2 * k2 + (a + 1) * k + (c + 1);
+            const int hhi = min(hip, base2 - 1), tlo = max(lop, base2 + k);
+            double hd = (lop + lane <= hhi) ? m0[(lop + lane) * st] : 0.0;
+            double tl = (tlo + lane <= hip) ? m0[(tlo + lane) * st + k2] : 0.0;
+            const int iv = base2 + lane;
+            const bool in = lane < k && iv >= lop && iv <= hip;
+            double ip = in ? m0[iv * st] : 0.0, is = in ? m0[iv * st + k2] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                hd += __shfl_xor_sync(FULL, hd, o);
+                tl += __shfl_xor_sync(FULL, tl, o);
+            }
+            for (int o = 1; o < 32; o <<= 1) {  // inclusive prefix (m) and suffix (M)
+                const double y = __shfl_up_sync(FULL, ip, o);
+                const double z = __shfl_down_sync(FULL, is, o);
+                if (lane >= o) ip += y;
+                if (lane + o < 32) is += z;
+            }
+            double ep = __shfl_up_sync(FULL, ip, 1), es = __shfl_down_sync(FULL, is, 1);
+            if (lane == 0) ep = 0.0;
+            if (lane == 31) es = 0.0;
+            pm = hd + ep;  // sum over iv1 < iv2_j
+            sm = tl + es;  // sum over iv1 > iv2_j
+        }
+        if (lane < k) {
+            s[lane * W + off] = pm;        // Pm
+            s[(k + lane) * W + off] = sm;  // SM
+        }
+    }
     // (b, d) part: one thread per (offset, j)
-    for (int x = threadIdx.x; x < W + W * k; x += blockDim.x) {
-        const bool ac = x < W;
-        const int y = ac ? x : x - W;
-        const int off = ac ? y : y / k, j = ac ? 0 : y - off * k;
+    for (int x = threadIdx.x; x < W * k; x += blockDim.x) {
+        const int off = x / k, j = x - off * k;
         const int iv2 = base2 + j;
         double v0 = 0.0, v1 = 0.0;
-        if (ac) {
-            const int c = a + off - (k - 1);
-            if (c >= 0 && c < N) {
-                const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-                const double *m0 = mom + (size_t)kk * 2 * k2 + (a + 1) * k + (c + 1);
-                // moment of interval iv1: m0[iv1 * (K1 2 k^2 - k - 1)] (+ k^2 for M)
-                const size_t st = (size_t)K1 * 2 * k2 - (size_t)(k + 1);
-                double pm = 0.0;  // sum over iv1 < iv2_j
-                for (int iv1 = lop; iv1 <= min(hip, base2 - 1); ++iv1) pm += m0[iv1 * st];
-                for (int jj = 0; jj < k; ++jj) {
-                    s[jj * W + off] = pm;  // Pm
-                    const int iv = base2 + jj;
-                    if (iv >= lop && iv <= hip) pm += m0[iv * st];
-                }
-                double sm = 0.0;  // sum over iv1 > iv2_j
-                for (int iv1 = hip; iv1 >= max(lop, base2 + k); --iv1) sm += m0[iv1 * st + k2];
-                for (int jj = k - 1; jj >= 0; --jj) {
-                    s[(k + jj) * W + off] = sm;  // SM
-                    const int iv = base2 + jj;
-                    if (iv >= lop && iv <= hip) sm += m0[iv * st + k2];
-                }
-            } else {
-                for (int jj = 0; jj < k; ++jj) {
-                    s[jj * W + off] = 0.0;
-                    s[(k + jj) * W + off] = 0.0;
-                }
-            }
-        } else {
+        {
             const int d = b + off - (k - 1);
             if (d >= 0 && d < N) {
                 const int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
@@ -371,6 +381,8 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
                 // the FP64 multiply; bs2e_dmul.h says why)
                 const double *x1 = P.tot + lower + (size_t)a * W + dc;
                 const double *x2 = P.tot + upper + (size_t)b * W + dd;
+                // independent multipoles: unrolled so the integer chains overlap
+#pragma unroll 4
                 for (int kk = k_first; kk < k_first + k_count; ++kk)
                     o[kk * W2] = dmul_int(x1[kk * NW], x2[kk * NW]);
             }

@@ -148,6 +148,44 @@ module bs2e_gpu
             integer(c_int64_t), value :: out_on_device
         end function
 
+        ! n1 bands of a block (rows of every channel with n1 in
+        ! [n1_first, n1_first + n1_count)), for blocks larger than memory:
+        ! sizes (and, with per_n1, (rows, nnz_H, nnz_S) per n1), then the
+        ! band's CSR and its 1-based block rows into host arrays
+        ! (out_on_device = 0) or device arrays (1).
+        integer(c_int32_t) function bs2e_block_band_count(h, configs, n_config, L, spin, full, &
+                n1_first, n1_count, n_rows, nnz_H, nnz_S, per_n1) &
+                bind(C, name="bs2e_block_band_count")
+            import :: c_int32_t, c_int64_t, c_ptr, bs2e_config_c
+            type(c_ptr), value :: h
+            type(bs2e_config_c), intent(in) :: configs(*)
+            integer(c_int64_t), value :: n_config, L, spin, full, n1_first, n1_count
+            integer(c_int64_t), intent(out) :: n_rows, nnz_H, nnz_S
+            integer(c_int64_t), intent(out) :: per_n1(*)
+        end function
+
+        integer(c_int32_t) function bs2e_block_fill_band(h, configs, n_config, L, spin, full, &
+                n1_first, n1_count, rows, H_index_ptr, H_indices, H_data, S_index_ptr, &
+                S_indices, S_data, out_on_device) bind(C, name="bs2e_block_fill_band")
+            import :: c_int32_t, c_int64_t, c_double_complex, c_ptr, bs2e_config_c
+            type(c_ptr), value :: h
+            type(bs2e_config_c), intent(in) :: configs(*)
+            integer(c_int64_t), value :: n_config, L, spin, full, n1_first, n1_count
+            integer(c_int64_t), intent(out) :: rows(*), H_index_ptr(*), H_indices(*)
+            complex(c_double_complex), intent(out) :: H_data(*)
+            integer(c_int64_t), intent(out) :: S_index_ptr(*), S_indices(*)
+            complex(c_double_complex), intent(out) :: S_data(*)
+            integer(c_int64_t), value :: out_on_device
+        end function
+
+        ! counted blocks the handle keeps (0..16); 0 recounts every block
+        integer(c_int32_t) function bs2e_set_block_cache(h, n_blocks) &
+                bind(C, name="bs2e_set_block_cache")
+            import :: c_int32_t, c_int64_t, c_ptr
+            type(c_ptr), value :: h
+            integer(c_int64_t), value :: n_blocks
+        end function
+
         ! CSR_mv (op 0), CSR_T_mv (op 1), CSR_mv_sym (op 2) of a type(CSR_matrix)
         integer(c_int32_t) function bs2e_csr_mv(h, op, n_rows, n_cols, nnz, index_ptr, indices, &
                 data, x, y, on_device) bind(C, name="bs2e_csr_mv")

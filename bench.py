@@ -71,7 +71,8 @@ WORKLOADS = {"order9_n800": LARGE, "order7_n200": MEDIUM}
 # DRAM bytes per algorithmic byte of the band fill, from one ncu capture of
 # one band of the large form per precision (the figures and the command are
 # in the profile summaries kept with this repository); None until captured.
-FILL_TRAFFIC_RATIO = {"order9_n800": {"fp64": None, "mixed": None},
+FILL_TRAFFIC_RATIO = {"order9_n800": {"fp64": (23052800.0 + 2262179000.0) / 2342289120.0,
+                                      "mixed": (25177600.0 + 2264250000.0) / 2342289120.0},
                       "order7_n200": {"fp64": 3478840576.0 / 3453526224.0,
                                       "mixed": 3683740672.0 / 3453526224.0}}
 
