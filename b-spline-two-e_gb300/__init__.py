@@ -45,7 +45,8 @@ EXPORTS = [
     "bs2e_rk_get_batch_static", "bs2e_write_block_diag", "bs2e_write_block",
     "bs2e_csr_mv", "bs2e_block_count_rows", "bs2e_block_fill_rows", "bs2e_rk_export",
     "bs2e_batch_create", "bs2e_batch_run", "bs2e_batch_tuning", "bs2e_batch_destroy",
-    "bs2e_csr_from_blocks",
+    "bs2e_csr_from_blocks", "bs2e_block_band_count", "bs2e_block_fill_band",
+    "bs2e_set_block_cache", "bs2e_band_plan", "bs2e_band_rows", "bs2e_band_merge",
 ]
 
 
