@@ -265,53 +265,24 @@ __device__ void rk_near_stage(const RadialDev &P, int a, int b, int kk, double *
     const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
     const int base2 = b - k + 2;
     const double *__restrict__ mom = P.mom;
-    // (a, c) part: one warp per offset; lane j takes the moments of interval
-    // iv2_j, lanes also take the head (iv1 < iv2_0) and tail (iv1 > iv2_{k-1})
-    // terms, and shuffle scans give Pm (exclusive prefix) and SM (exclusive
-    // suffix); all additions are of positive terms
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const size_t st = (size_t)K1 * 2 * k2 - (size_t)(k + 1);  // interval stride of mom
-    for (int off = warp; off < W; off += nwarp) {
-        const int c = a + off - (k - 1);
-        double pm = 0.0, sm = 0.0;
-        if (c >= 0 && c < N) {  // warp-uniform
-            const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-            // moment of interval iv1: m0[iv1 * st] (+ k^2 for M)
-            const double *m0 = mom + (size_t)kk * 2 * k2 + (a + 1) * k + (c + 1);
-            const int hhi = min(hip, base2 - 1), tlo = max(lop, base2 + k);
-            double hd = (lop + lane <= hhi) ? m0[(lop + lane) * st] : 0.0;
-            double tl = (tlo + lane <= hip) ? m0[(tlo + lane) * st + k2] : 0.0;
-            const int iv = base2 + lane;
-            const bool in = lane < k && iv >= lop && iv <= hip;
-            double ip = in ? m0[iv * st] : 0.0, is = in ? m0[iv * st + k2] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) {
-                hd += __shfl_xor_sync(FULL, hd, o);
-                tl += __shfl_xor_sync(FULL, tl, o);
-            }
-            for (int o = 1; o < 32; o <<= 1) {  // inclusive prefix (m) and suffix (M)
-                const double y = __shfl_up_sync(FULL, ip, o);
-                const double z = __shfl_down_sync(FULL, is, o);
-                if (lane >= o) ip += y;
-                if (lane + o < 32) is += z;
-            }
-            double ep = __shfl_up_sync(FULL, ip, 1), es = __shfl_down_sync(FULL, is, 1);
-            if (lane == 0) ep = 0.0;
-            if (lane == 31) es = 0.0;
-            pm = hd + ep;  // sum over iv1 < iv2_j
-            sm = tl + es;  // sum over iv1 > iv2_j
-        }
-        if (lane < k) {
-            s[lane * W + off] = pm;        // Pm
-            s[(k + lane) * W + off] = sm;  // SM
-        }
-    }
-    // (b, d) part: one thread per (offset, j)
-    for (int x = threadIdx.x; x < W * k; x += blockDim.x) {
-        const int off = x / k, j = x - off * k;
+    for (int x = threadIdx.x; x < 2 * W * k; x += blockDim.x) {
+        const bool ac = x < W * k;
+        const int y = ac ? x : x - W * k;
+        const int off = y / k, j = y - off * k;
         const int iv2 = base2 + j;
         double v0 = 0.0, v1 = 0.0;
-        {
+        if (ac) {
+            const int c = a + off - (k - 1);
+            if (c >= 0 && c < N) {
+                const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
+                for (int iv1 = lop; iv1 <= min(hip, iv2 - 1); ++iv1)
+                    v0 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+                for (int iv1 = max(lop, iv2 + 1); iv1 <= hip; ++iv1)
+                    v1 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+            }
+            s[j * W + off] = v0;          // Pm
+            s[(k + j) * W + off] = v1;    // SM
+        } else {
             const int d = b + off - (k - 1);
             if (d >= 0 && d < N) {
                 const int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);

@@ -302,7 +302,7 @@ class LargeJob:
         self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
         # the consumer: a second handle (any basis; it only runs the mat-vec on
         # device pointers) whose stream works while the next band fills
-        self.hc = pkg.Bs2e(pkg.grids.explin_knots(4, 8, 10.0), 4, 4, 0, device=self.dev.index)
+        self.hc = pkg.Bs2e(pkg.grids.explin_knots(6, 24, 20.0), 6, 8, 0, device=self.dev.index)
         self.cstream = torch.cuda.ExternalStream(self.hc.stream, device=self.dev)
         self.areas = areas
         self.blocks = [(L, M, par, spin, self._pin(cf)) for (L, M, par, spin, cf)
