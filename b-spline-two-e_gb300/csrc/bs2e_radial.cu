@@ -305,7 +305,11 @@ __device__ __forceinline__ double rk_near_element(const RadialDev &P, const doub
     const int c = a + dc - (k - 1), d = b + dd - (k - 1);
     if (c < 0 || c >= N || d < 0 || d >= N) return 0.0;
     double v = 0.0;
-    for (int j = 0; j < k; ++j) {
+    // m(bd) and M(bd) vanish off the (b, d) pair's intervals, iv2_j in
+    // [max(b, d) - k + 2, min(b, d) + 1]: the terms skipped there are exact
+    // zeros, so the sum is the same bit for bit
+    const int jlo = max(0, d - b), jhi = k - 1 + min(0, d - b);
+    for (int j = jlo; j <= jhi; ++j) {
         v = fma(s[(3 * k + j) * W + dd], s[j * W + dc], v);
         v = fma(s[(2 * k + j) * W + dd], s[(k + j) * W + dc], v);
     }
@@ -319,12 +323,15 @@ __device__ __forceinline__ double rk_near_element(const RadialDev &P, const doub
     return v;
 }
 
-__host__ __device__ __forceinline__ size_t rk_near_scratch(int k) {
-    return (size_t)4 * k * (2 * k - 1);  // doubles
+// Scratch doubles of a tile: the near-field stage s[4][k][W] or the far-field
+// pair totals [2][K1][W].
+__host__ __device__ __forceinline__ size_t rk_scratch(int k, int K1) {
+    const size_t W = 2 * k - 1, near = 4 * (size_t)k * W, far = 2 * (size_t)K1 * W;
+    return near > far ? near : far;
 }
 
 // Values of multipoles [k_first, k_first + k_count) of tile t = a * N + b:
-// out[kk * W^2 + dc * W + dd] (block-wide; s: rk_near_scratch doubles).  Each
+// out[kk * W^2 + dc * W + dd] (block-wide; s: rk_scratch doubles).  Each
 // thread keeps its window positions r = dc * W + dd (r = threadIdx.x + i *
 // blockDim.x) and walks them with an incremental (dc, dd), so no element pays
 // an integer division.
@@ -337,31 +344,42 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
     if (abs(a - b) >= k) {
         // far field everywhere: the (a, c) intervals lie all below the (b, d)
         // ones when a < b, all above when a > b, so R^k is the product of the
-        // pair totals, m_k(ac) M_k(bd) or M_k(ac) m_k(bd)
-        // (sparse_array_tools.f90:452-493 sums the same interval products)
+        // pair totals, X = m_k(ac) and Y = M_k(bd), or X = M_k(ac) and
+        // Y = m_k(bd) (sparse_array_tools.f90:452-493 sums the same interval
+        // products).  The totals are 0 where c or d falls off the grid, so
+        // those elements come out as +0.
         const size_t NW = (size_t)N * W, lower = a < b ? 0 : (size_t)K1 * NW;
         const size_t upper = a < b ? (size_t)K1 * NW : 0;
-        int dc = dc0, dd = dd0;
-        for (int r = threadIdx.x; r < W2; r += blockDim.x) {
-            const int c = a + dc - (k - 1), d = b + dd - (k - 1);
-            double *o = out + r;
-            if (c < 0 || c >= N || d < 0 || d >= N) {
-                for (int kk = k_first; kk < k_first + k_count; ++kk) o[kk * W2] = 0.0;
-            } else {
-                // one product per element, on the integer pipes (bit for bit
-                // the FP64 multiply; bs2e_dmul.h says why)
-                const double *x1 = P.tot + lower + (size_t)a * W + dc;
-                const double *x2 = P.tot + upper + (size_t)b * W + dd;
-                // independent multipoles: unrolled so the integer chains overlap
-#pragma unroll 4
-                for (int kk = k_first; kk < k_first + k_count; ++kk)
-                    o[kk * W2] = dmul_int(x1[kk * NW], x2[kk * NW]);
+        double *sx = s, *sy = s + (size_t)K1 * W;  // [K1][W] each
+        for (int i = threadIdx.x; i < k_count * W; i += blockDim.x) {
+            const int kq = i / W, off = i - kq * W, kk = k_first + kq;
+            sx[kk * W + off] = P.tot[lower + kk * NW + (size_t)a * W + off];
+            sy[kk * W + off] = P.tot[upper + kk * NW + (size_t)b * W + off];
+        }
+        __syncthreads();
+        // every thread walks elements e = kk W^2 + dc W + dd, blockDim apart,
+        // with an incremental (kk, dc, dd); one product per stored element,
+        // odd warps on the integer pipes (bit for bit the FP64 multiply;
+        // bs2e_dmul.h says why) and even warps on the FP64 pipe, so the two
+        // pipes share the products
+        const int S = blockDim.x, sk = S / W2, sdc = (S - sk * W2) / W;
+        const int sdd = S - sk * W2 - sdc * W;
+        const int e1 = (k_first + k_count) * W2;
+        int e = k_first * W2 + threadIdx.x;
+        int kk = e / W2, dc = (e - kk * W2) / W, dd = e - kk * W2 - dc * W;
+        if ((threadIdx.x >> 5) & 1) {
+            for (; e < e1; e += S) {
+                out[e] = dmul_int(sx[kk * W + dc], sy[kk * W + dd]);
+                kk += sk; dc += sdc; dd += sdd;
+                if (dd >= W) { dd -= W; ++dc; }
+                if (dc >= W) { dc -= W; ++kk; }
             }
-            dc += step_dc;
-            dd += step_dd;
-            if (dd >= W) {
-                dd -= W;
-                ++dc;
+        } else {
+            for (; e < e1; e += S) {
+                out[e] = sx[kk * W + dc] * sy[kk * W + dd];
+                kk += sk; dc += sdc; dd += sdd;
+                if (dd >= W) { dd -= W; ++dc; }
+                if (dc >= W) { dc -= W; ++kk; }
             }
         }
         return;
@@ -430,7 +448,7 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
 }
 
 __global__ void k_rk_store(RadialDev P, int k_first, int k_count) {
-    extern __shared__ double scr[];  // rk_near_scratch(k) doubles
+    extern __shared__ double scr[];  // rk_scratch(k, K1) doubles
     rk_tile_fp64(P, blockIdx.x, k_first, k_count, scr);
 }
 
@@ -744,7 +762,7 @@ void launch_totals(bs2e_handle *h) {
 }
 
 size_t rk_store_smem(const Radial &g, bool mixed) {
-    return sizeof(double) * (rk_near_scratch(g.k) + (mixed ? (size_t)g.K1 * g.W * g.W : 0));
+    return sizeof(double) * (rk_scratch(g.k, g.K1) + (mixed ? (size_t)g.K1 * g.W * g.W : 0));
 }
 
 void launch_rk_fill(bs2e_handle *h, int k_first, int k_count) {
