@@ -40,7 +40,8 @@ EXPORTS = [
     "bs2e_set_one_body", "bs2e_one_body", "bs2e_block_count", "bs2e_block_fill",
     "bs2e_block_count_ex", "bs2e_block_fill_ex", "bs2e_blocks_count_all",
     "bs2e_blocks_fill_all", "bs2e_configs", "bs2e_ang_k_LS",
-    "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_launch_count", "bs2e_synchronize",
+    "bs2e_three_j", "bs2e_six_j", "bs2e_stream", "bs2e_set_stream_priority",
+    "bs2e_launch_count", "bs2e_synchronize",
     "bs2e_radial_dipole", "bs2e_set_radial_dipole", "bs2e_dip_block_count", "bs2e_dip_block_fill",
     "bs2e_rk_get_batch_static", "bs2e_write_block_diag", "bs2e_write_block",
     "bs2e_csr_mv", "bs2e_block_count_rows", "bs2e_block_fill_rows", "bs2e_rk_export",
@@ -117,6 +118,7 @@ def lib():
         "bs2e_three_j": (dbl, [i64, i64, i64, i64, i64, i64]),
         "bs2e_six_j": (dbl, [i64, i64, i64, i64, i64, i64]),
         "bs2e_stream": (st, [p, p]),
+        "bs2e_set_stream_priority": (st, [p, i64]),
         "bs2e_launch_count": (st, [p, p]),
         "bs2e_synchronize": (st, [p]),
         "bs2e_radial_dipole": (st, [p, i64, p, p, p]),
@@ -655,6 +657,11 @@ class Bs2e:
         s = ctypes.c_void_p()
         _check(self._h, lib().bs2e_stream(self._h, ctypes.byref(s)))
         return s.value
+
+    def set_stream_priority(self, priority):
+        """Recreate the handle's stream with this CUDA stream priority (smaller
+        is higher; see torch.cuda.Stream.priority_range())."""
+        _check(self._h, lib().bs2e_set_stream_priority(self._h, int(priority)))
 
     @property
     def launch_count(self):

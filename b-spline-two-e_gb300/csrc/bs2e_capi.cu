@@ -1627,6 +1627,21 @@ BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream) {
     return BS2E_OK;
 }
 
+BS2E_API bs2e_status bs2e_set_stream_priority(bs2e_handle *h, int64_t priority) {
+    if (!h) return BS2E_ERR_ARG;
+    Guard g(h);
+    int lo = 0, hi = 0;  // CUDA's range: lo is the lowest priority, hi the highest
+    CU(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    if (priority > lo || priority < hi)
+        return fail(h, BS2E_ERR_ARG, "set_stream_priority: outside the device's priority range");
+    cudaStream_t s = nullptr;
+    CU(cudaStreamSynchronize(h->stream));
+    CU(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, (int)priority));
+    cudaStreamDestroy(h->stream);
+    h->stream = s;
+    return BS2E_OK;
+}
+
 BS2E_API bs2e_status bs2e_launch_count(const bs2e_handle *h, int64_t *count) {
     if (!h || !count) return BS2E_ERR_ARG;
     *count = h->launches;

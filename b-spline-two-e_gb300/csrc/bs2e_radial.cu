@@ -260,12 +260,15 @@ __global__ void k_totals(RadialDev P) {
 //       + sum_{shared iv} D(iv; ac, bd) + D(iv; bd, ac),
 // 2k FMAs per element instead of up to k^2 products.  Both sums add
 // positive moments (B-splines are non-negative), so the regrouping keeps full
-// accuracy.  Staged per multipole in s[4][k][W]: Pm, SM over dc; m, M over dd.
-__device__ void rk_near_stage(const RadialDev &P, int a, int b, int kk, double *s) {
+// accuracy.  Staged per multipole in s[4][k][W]: Pm, SM over dc; m, M over dd;
+// multipoles [g0, g0 + gn) at once, multipole g0 + i at s + i * 4kW.
+__device__ void rk_near_stage(const RadialDev &P, int a, int b, int g0, int gn, double *sg) {
     const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
-    const int base2 = b - k + 2;
+    const int base2 = b - k + 2, per = 2 * W * k;
     const double *__restrict__ mom = P.mom;
-    for (int x = threadIdx.x; x < 2 * W * k; x += blockDim.x) {
+    for (int xg = threadIdx.x; xg < gn * per; xg += blockDim.x) {
+        const int gi = xg / per, x = xg - gi * per, kk = g0 + gi;
+        double *s = sg + (size_t)gi * 2 * per;
         const bool ac = x < W * k;
         const int y = ac ? x : x - W * k;
         const int off = y / k, j = y - off * k;
@@ -323,24 +326,33 @@ __device__ __forceinline__ double rk_near_element(const RadialDev &P, const doub
     return v;
 }
 
-// Scratch doubles of a tile: the near-field stage s[4][k][W] or the far-field
-// pair totals [2][K1][W].
+// Multipoles staged together in a near-field tile: as many stages s[4][k][W]
+// as fit in about 20 KB, so a tile takes few barrier pairs and every thread
+// has elements to compute.
+__host__ __device__ __forceinline__ int rk_near_group(int k, int K1) {
+    const int one = 4 * k * (2 * k - 1), g = 2560 / one;
+    return g < 1 ? 1 : (g > K1 ? K1 : g);
+}
+
+// Scratch doubles of a tile: the near-field stages of a group or the
+// far-field pair totals [2][K1][W].
 __host__ __device__ __forceinline__ size_t rk_scratch(int k, int K1) {
-    const size_t W = 2 * k - 1, near = 4 * (size_t)k * W, far = 2 * (size_t)K1 * W;
+    const size_t W = 2 * k - 1, near = 4 * (size_t)k * W * rk_near_group(k, K1);
+    const size_t far = 2 * (size_t)K1 * W;
     return near > far ? near : far;
 }
 
 // Values of multipoles [k_first, k_first + k_count) of tile t = a * N + b:
 // out[kk * W^2 + dc * W + dd] (block-wide; s: rk_scratch doubles).  Each
-// thread keeps its window positions r = dc * W + dd (r = threadIdx.x + i *
-// blockDim.x) and walks them with an incremental (dc, dd), so no element pays
-// an integer division.
+// thread takes the elements blockDim apart from its own and walks them with an
+// incremental (kk, dc, dd), so no element pays an integer division.
 __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k_count,
                                double *out, double *s) {
     const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
     const int a = (int)(t / N), b = (int)(t - (int64_t)a * N);
-    const int step_dc = blockDim.x / W, step_dd = blockDim.x - step_dc * W;
-    const int dc0 = threadIdx.x / W, dd0 = threadIdx.x - dc0 * W;
+    // a thread's elements lie blockDim apart: that stride as (multipoles, dc, dd)
+    const int S = blockDim.x, sk = S / W2, sdc = (S - sk * W2) / W;
+    const int sdd = S - sk * W2 - sdc * W;
     if (abs(a - b) >= k) {
         // far field everywhere: the (a, c) intervals lie all below the (b, d)
         // ones when a < b, all above when a > b, so R^k is the product of the
@@ -362,8 +374,6 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
         // odd warps on the integer pipes (bit for bit the FP64 multiply;
         // bs2e_dmul.h says why) and even warps on the FP64 pipe, so the two
         // pipes share the products
-        const int S = blockDim.x, sk = S / W2, sdc = (S - sk * W2) / W;
-        const int sdd = S - sk * W2 - sdc * W;
         const int e1 = (k_first + k_count) * W2;
         int e = k_first * W2 + threadIdx.x;
         int kk = e / W2, dc = (e - kk * W2) / W, dd = e - kk * W2 - dc * W;
@@ -384,19 +394,26 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
         }
         return;
     }
-    for (int kk = k_first; kk < k_first + k_count; ++kk) {
+    const int G = rk_near_group(k, K1), per = 4 * k * W;
+    for (int g0 = k_first; g0 < k_first + k_count; g0 += G) {
+        const int gn = min(G, k_first + k_count - g0);
+        __syncthreads();  // the previous group's elements are done with s
+        rk_near_stage(P, a, b, g0, gn, s);
         __syncthreads();
-        rk_near_stage(P, a, b, kk, s);
-        __syncthreads();
-        int dc = dc0, dd = dd0;
-        for (int r = threadIdx.x; r < W2; r += blockDim.x) {
-            out[kk * W2 + r] = rk_near_element(P, s, a, b, kk, dc, dd);
-            dc += step_dc;
-            dd += step_dd;
-            if (dd >= W) {
-                dd -= W;
-                ++dc;
-            }
+        // the group's elements taken in the order (dd, multipole, dc), so the
+        // lanes of a warp mostly share dd: both loops of rk_near_element run
+        // over intervals of the (b, d) pair, and with d common their trip
+        // counts agree across the warp instead of every lane waiting for the
+        // longest (the stores go out W apart, on these few tiles only)
+        const int GW = gn * W, tdd = S / GW, tgi = (S - tdd * GW) / W;
+        const int tdc = S - tdd * GW - tgi * W;
+        int e = threadIdx.x, dd = e / GW, gi = (e - dd * GW) / W, dc = e - dd * GW - gi * W;
+        for (; e < gn * W2; e += S) {
+            out[(size_t)(g0 + gi) * W2 + dc * W + dd] =
+                rk_near_element(P, s + (size_t)gi * per, a, b, g0 + gi, dc, dd);
+            dd += tdd; gi += tgi; dc += tdc;
+            if (dc >= W) { dc -= W; ++gi; }
+            if (gi >= gn) { gi -= gn; ++dd; }
         }
     }
 }

@@ -186,6 +186,14 @@ module bs2e_gpu
             integer(c_int64_t), value :: n_blocks
         end function
 
+        ! recreate the handle's stream with a CUDA stream priority (smaller is higher)
+        integer(c_int32_t) function bs2e_set_stream_priority(h, priority) &
+                bind(C, name="bs2e_set_stream_priority")
+            import :: c_int32_t, c_int64_t, c_ptr
+            type(c_ptr), value :: h
+            integer(c_int64_t), value :: priority
+        end function
+
         ! CSR_mv (op 0), CSR_T_mv (op 1), CSR_mv_sym (op 2) of a type(CSR_matrix)
         integer(c_int32_t) function bs2e_csr_mv(h, op, n_rows, n_cols, nnz, index_ptr, indices, &
                 data, x, y, on_device) bind(C, name="bs2e_csr_mv")

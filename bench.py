@@ -301,8 +301,11 @@ class LargeJob:
         self.h.set_block_cache(0)
         self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
         # the consumer: a second handle (any basis; it only runs the mat-vec on
-        # device pointers) whose stream works while the next band fills
+        # device pointers) whose stream works while the next band fills, at
+        # the highest stream priority so its CTAs take SM slots as fill CTAs
+        # retire instead of waiting for the whole band
         self.hc = pkg.Bs2e(pkg.grids.explin_knots(6, 24, 20.0), 6, 8, 0, device=self.dev.index)
+        self.hc.set_stream_priority(torch.cuda.Stream.priority_range()[1])
         self.cstream = torch.cuda.ExternalStream(self.hc.stream, device=self.dev)
         self.areas = areas
         self.blocks = [(L, M, par, spin, self._pin(cf)) for (L, M, par, spin, cf)

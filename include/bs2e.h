@@ -461,6 +461,15 @@ BS2E_API bs2e_status bs2e_batch_destroy(bs2e_batch *b);
  * event) when the call is made.  Every entry point has finished its device
  * work on this stream when it returns. */
 BS2E_API bs2e_status bs2e_stream(bs2e_handle *h, void **stream);
+
+/* Recreates the handle's stream with a CUDA stream priority (a smaller number
+ * is a higher priority; cudaDeviceGetStreamPriorityRange gives the range,
+ * values outside it are refused with BS2E_ERR_ARG).  Waits for the handle's
+ * work first; bs2e_stream returns the new stream afterwards.  For a handle
+ * whose kernels should take SM slots ahead of another's, e.g. one that applies
+ * bands while a second handle fills the next ones.  No counterpart in the
+ * reference. */
+BS2E_API bs2e_status bs2e_set_stream_priority(bs2e_handle *h, int64_t priority);
 BS2E_API bs2e_status bs2e_launch_count(const bs2e_handle *h, int64_t *count);
 BS2E_API bs2e_status bs2e_synchronize(bs2e_handle *h);
 

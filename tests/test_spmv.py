@@ -234,3 +234,29 @@ def test_gpu_mv_columns_8_byte_aligned(bs2e, oracle):
             h.csr_mv_device(0, 200, 150, A["nnz"], ptr.data_ptr(), idx.data_ptr(),
                             dat.data_ptr(), xd.data_ptr(), yd.data_ptr())
             _check(yd.cpu().numpy(), want, scale)
+
+
+@pytest.mark.gpu
+def test_stream_priority_keeps_products(bs2e, oracle):
+    """bs2e_set_stream_priority recreates the handle's stream (a new stream,
+    same products); priorities outside the device's range are refused and
+    leave the handle usable."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    A = _random_csr(rng, 120, 90, 0.1)
+    x = rng.standard_normal(90) + 1j * rng.standard_normal(90)
+    want, scale = oracle.csr_mv(0, A["shape"], A["index_ptr"], A["indices"], A["data"], x)
+    least, greatest = torch.cuda.Stream.priority_range()
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
+        s0 = h.stream
+        h.set_stream_priority(greatest)
+        assert h.stream != s0
+        _check(h.csr_mv(A, x, 0), want, scale)
+        # torch's range may be narrower than the device's; these are outside both
+        with pytest.raises(bs2e.Bs2eError, match="priority range"):
+            h.set_stream_priority(-1000)
+        with pytest.raises(bs2e.Bs2eError, match="priority range"):
+            h.set_stream_priority(1000)
+        h.set_stream_priority(least)
+        _check(h.csr_mv(A, x, 0), want, scale)
