@@ -1178,7 +1178,10 @@ __global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS :
     __shared__ int sexp[kMaxK1];
     __shared__ float2 sA[4][2][kMaxK1];
     __shared__ int sKo[4][2][kMaxK1];
-    __shared__ int srow[kMaxCh], sch[kMaxCh], snrow;
+    __shared__ int srow[kMaxCh], sch[kMaxCh], snrow, snext;
+    __shared__ int snz[kMaxCh];
+    __shared__ uint8_t sord[kMaxCh];
+    static_assert(kMaxCh <= 256, "row order kept in bytes");
     const BlockArgs &A = F.B;
     const int n_a = F.a0 + (int)(blockIdx.x / A.N), n_b = blockIdx.x % A.N + 1;
     const size_t tix = (size_t)(n_a - 1) * A.N + (n_b - 1);
@@ -1214,10 +1217,31 @@ __global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS :
     if (MIXED) {
         for (int i = threadIdx.x; i < A.K1; i += blockDim.x) sexp[i] = F.Rexp[tix * A.K1 + i];
     }
+    // rows by descending H entry count (a rank sort), handed out one at a
+    // time below, so a warp that finishes early takes the next row instead of
+    // idling while the others work through an unequal round-robin share
+    for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+        const int64_t n = F.Hptr[srow[i] + 1] - F.Hptr[srow[i]];
+        snz[i] = (int)min(n, (int64_t)0x7fffffff);
+    }
+    if (threadIdx.x == 0) snext = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nrow; i += blockDim.x) {
+        int r = 0;
+        for (int j = 0; j < nrow; ++j) r += snz[j] > snz[i] || (snz[j] == snz[i] && j < i);
+        sord[r] = (uint8_t)i;
+    }
+    // (stage_tile begins with a barrier, which orders sord before its use)
     if (!stage_tile(src, sR, (uint32_t)(F.tile * sizeof(double)), &bar, F.err)) return;
-    const int warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int rr = warp; rr < nrow; rr += nwarp)
-        fill_row<MIXED, BIG>(F, srow[rr], sch[rr], n_a, n_b, sR, sexp, sA[warp], sKo[warp]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (;;) {
+        int rr = 0;
+        if (lane == 0) rr = atomicAdd(&snext, 1);
+        rr = __shfl_sync(0xffffffffu, rr, 0);
+        if (rr >= nrow) break;
+        const int i = sord[rr];
+        fill_row<MIXED, BIG>(F, srow[i], sch[i], n_a, n_b, sR, sexp, sA[warp], sKo[warp]);
+    }
 }
 
 // Row mode, for row ranges inside one or two channels, where a tile holds a
