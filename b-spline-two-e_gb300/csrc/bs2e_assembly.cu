@@ -490,19 +490,15 @@ __device__ __forceinline__ FF ff_join(FF a, int Ea, bool has_a, FF b, int Eb, bo
 #ifndef BS2E_FILL_MIN_BLOCKS_FP64
 #define BS2E_FILL_MIN_BLOCKS_FP64 8
 #endif
-// The large-tile variant (R^k tiles above ~22 KB): resident CTAs per SM it is
-// compiled for, and entries per lane of its FP64 loop.  Measured on four
-// order-9 N=800 bands (k=0..20, l_max=10; 2.1e9 entries): 2 entries, 4 CTAs
-// -> 19.7 ms (120 registers); 4 entries, 4 CTAs -> 21.0 (118); 4 entries,
-// 3 CTAs -> 21.2 (142); 8 entries, 4 CTAs -> 28.5 (128).  The loop is bound
-// by FP64 issue, and a wider group runs more multipole FMAs for entries whose
-// sum is then dropped (outside sup or sup_x), so more chains per lane lose.
-#ifndef BS2E_FILL_MIN_BLOCKS_BIG
-#define BS2E_FILL_MIN_BLOCKS_BIG 4
-#endif
-#ifndef BS2E_FILL_ENTRIES_BIG
-#define BS2E_FILL_ENTRIES_BIG 2
-#endif
+// The large-tile variant (R^k tiles above ~22 KB) is compiled for 4 CTAs per
+// SM.  Its FP64 loop takes two entries per lane; measured on four order-9
+// N=800 bands (k=0..20, l_max=10; 2.1e9 entries) with the loop written for E
+// entries per lane: E=2, 4 CTAs -> 19.7 ms (120 registers); E=4, 4 CTAs ->
+// 21.0 (118); E=4, 3 CTAs -> 21.2 (142); E=8, 4 CTAs -> 28.5 (128).  The loop
+// is bound by FP64 issue, and a wider group runs more multipole FMAs for
+// entries whose sum is then dropped (outside sup or sup_x).  The generic
+// form also cost the small-tile kernel 2-3% (more spills), so the two-entry
+// loop stays written out.
 
 // Direct + exchange multipole sums of one entry in FP64 from the mixed store
 // (each stored pair rescaled exactly to its value), for channel pairs whose
@@ -728,108 +724,118 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, con
                 // "under sup" alone decides and the two-entry loop needs no
                 // per-entry test; a flagged block takes the gated loop below.
                 if (!MIXED && F.s_real && !F.gated) {
-                    // FP64 with a real S: E entries per lane (e, e + 32, ...
-                    // of each 32 E), so their run searches and multipole FMA
-                    // chains are independent and overlap; an entry outside
+                    // FP64 with a real S: two entries per lane (e and e + 32 of
+                    // each 64), so the two run searches and the two multipole
+                    // FMA chains are independent and overlap; an entry outside
                     // sup (sup_x) reads a valid tile element and drops the sum
-                    constexpr int E = BIG ? BS2E_FILL_ENTRIES_BIG : 2;
-                    for (int e0 = 0; e0 < tot; e0 += 32 * E) {
-                        int ev[E], pv[E];
-#pragma unroll
-                        for (int q = 0; q < E; ++q) {
-                            ev[q] = e0 + lane + 32 * q;
-                            pv[q] = 0;
-                        }
+                    for (int e0 = 0; e0 < tot; e0 += 64) {
+                        const int eA = e0 + lane, eB = eA + 32;
+                        int pA = 0, pB = 0;
 #pragma unroll
                         for (int step = 16; step > 0; step >>= 1) {
-#pragma unroll
-                            for (int q = 0; q < E; ++q) {
-                                const int v = __shfl_sync(FULL, excl, pv[q] + step);
-                                if (v <= ev[q]) pv[q] += step;
-                            }
+                            const int vA = __shfl_sync(FULL, excl, pA + step);
+                            const int vB = __shfl_sync(FULL, excl, pB + step);
+                            if (vA <= eA) pA += step;
+                            if (vB <= eB) pB += step;
                         }
-                        int nc[E], nd[E], jv[E];
-                        bool live[E], sup[E], supx[E];
-                        bool any_d = false, any_x = false;
-#pragma unroll
-                        for (int q = 0; q < E; ++q) {
-                            const int o = ev[q] - __shfl_sync(FULL, excl, pv[q]);
-                            const int l1 = __shfl_sync(FULL, hs.l1, pv[q]);
-                            const int s1 = __shfl_sync(FULL, hs.s1, pv[q]);
-                            const int s2 = __shfl_sync(FULL, hs.s2, pv[q]);
-                            nc[q] = __shfl_sync(FULL, n_c, pv[q]);
-                            nd[q] = o < l1 ? s1 + o : s2 + (o - l1);
-                            jv[q] = __shfl_sync(FULL, base, pv[q]) + (nd[q] - __shfl_sync(FULL, lo, pv[q]));
-                            live[q] = ev[q] < tot;
-                            sup[q] = live[q] && abs(n_a - nc[q]) < k && abs(n_b - nd[q]) < k;
-                            supx[q] = live[q] && abs(n_a - nd[q]) < k && abs(n_b - nc[q]) < k;
-                            any_d |= sup[q];
-                            any_x |= supx[q];
+                        int ncA, ndA, jA, ncB, ndB, jB;
+                        {
+                            const int o = eA - __shfl_sync(FULL, excl, pA);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pA);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pA), s2 = __shfl_sync(FULL, hs.s2, pA);
+                            ncA = __shfl_sync(FULL, n_c, pA);
+                            ndA = o < l1 ? s1 + o : s2 + (o - l1);
+                            jA = __shfl_sync(FULL, base, pA) + (ndA - __shfl_sync(FULL, lo, pA));
                         }
-                        double re[E], im[E];
-#pragma unroll
-                        for (int q = 0; q < E; ++q) re[q] = im[q] = 0.0;
-                        if (any_d) {
-                            int ov[E];
-                            double acc[E];
-#pragma unroll
-                            for (int q = 0; q < E; ++q) {
-                                ov[q] = sup[q] ? (nc[q] - n_a + k - 1) * W + (nd[q] - n_b + k - 1) : 0;
-                                acc[q] = 0.0;
-                            }
+                        {
+                            const int o = eB - __shfl_sync(FULL, excl, pB);
+                            const int l1 = __shfl_sync(FULL, hs.l1, pB);
+                            const int s1 = __shfl_sync(FULL, hs.s1, pB), s2 = __shfl_sync(FULL, hs.s2, pB);
+                            ncB = __shfl_sync(FULL, n_c, pB);
+                            ndB = o < l1 ? s1 + o : s2 + (o - l1);
+                            jB = __shfl_sync(FULL, base, pB) + (ndB - __shfl_sync(FULL, lo, pB));
+                        }
+                        const bool liveA = eA < tot, liveB = eB < tot;
+                        const bool supA = liveA && abs(n_a - ncA) < k && abs(n_b - ndA) < k;
+                        const bool supxA = liveA && abs(n_a - ndA) < k && abs(n_b - ncA) < k;
+                        const bool supB = liveB && abs(n_a - ncB) < k && abs(n_b - ndB) < k;
+                        const bool supxB = liveB && abs(n_a - ndB) < k && abs(n_b - ncB) < k;
+                        double reA = 0.0, imA = 0.0, reB = 0.0, imB = 0.0;
+                        if (supA || supB) {
+                            const int oA = supA ? (ncA - n_a + k - 1) * W + (ndA - n_b + k - 1) : 0;
+                            const int oB = supB ? (ncB - n_a + k - 1) * W + (ndB - n_b + k - 1) : 0;
+                            double a = 0.0, b = 0.0;
 #pragma unroll 4
                             for (int u = 0; u < pi.nd; ++u) {
                                 const int ko = sKow[0][u];
                                 const double w = sAd[0][u];
-#pragma unroll
-                                for (int q = 0; q < E; ++q) acc[q] = fma(sR[ov[q] + ko], w, acc[q]);
+                                a = fma(sR[oA + ko], w, a);
+                                b = fma(sR[oB + ko], w, b);
                             }
-#pragma unroll
-                            for (int q = 0; q < E; ++q) re[q] = sup[q] ? acc[q] : 0.0;
+                            reA = supA ? a : 0.0;
+                            reB = supB ? b : 0.0;
                         }
-                        if (any_x) {
-                            int ov[E];
-                            double acc[E];
-#pragma unroll
-                            for (int q = 0; q < E; ++q) {
-                                ov[q] = supx[q] ? (nd[q] - n_a + k - 1) * W + (nc[q] - n_b + k - 1) : 0;
-                                acc[q] = re[q];
-                            }
+                        if (supxA || supxB) {
+                            const int oA = supxA ? (ndA - n_a + k - 1) * W + (ncA - n_b + k - 1) : 0;
+                            const int oB = supxB ? (ndB - n_a + k - 1) * W + (ncB - n_b + k - 1) : 0;
+                            double a = reA, b = reB;
 #pragma unroll 4
                             for (int u = 0; u < pi.nx; ++u) {
                                 const int ko = sKow[1][u];
                                 const double w = sAd[1][u];
-#pragma unroll
-                                for (int q = 0; q < E; ++q) acc[q] = fma(sR[ov[q] + ko], w, acc[q]);
+                                a = fma(sR[oA + ko], w, a);
+                                b = fma(sR[oB + ko], w, b);
                             }
-#pragma unroll
-                            for (int q = 0; q < E; ++q) re[q] = supx[q] ? acc[q] : re[q];
+                            reA = supxA ? a : reA;
+                            reB = supxB ? b : reB;
                         }
-#pragma unroll
-                        for (int q = 0; q < E; ++q) {
-                            if (leq && sup[q]) {
-                                const int dc = nc[q] - n_a, dd = nd[q] - n_b;
+                        if (leq) {
+                            if (supA) {
+                                const int dc = ncA - n_a, dd = ndA - n_b;
                                 const double2 h1 = HaR[dc], h2 = HbR[dd];
                                 const double s1 = SbR[dd].x, s2 = SaR[dc].x;
-                                re[q] = fma(h1.x, s1, re[q]);
-                                re[q] = fma(h2.x, s2, re[q]);
-                                im[q] = fma(h1.y, s1, im[q]);
-                                im[q] = fma(h2.y, s2, im[q]);
+                                reA = fma(h1.x, s1, reA);
+                                reA = fma(h2.x, s2, reA);
+                                imA = fma(h1.y, s1, imA);
+                                imA = fma(h2.y, s2, imA);
                             }
-                            if (leqx && supx[q]) {
-                                const int dc = nd[q] - n_a, dd = nc[q] - n_b;
+                            if (supB) {
+                                const int dc = ncB - n_a, dd = ndB - n_b;
                                 const double2 h1 = HaR[dc], h2 = HbR[dd];
-                                const double s1 = flip_sign(SbR[dd].x, sgn_bit);
-                                const double s2 = flip_sign(SaR[dc].x, sgn_bit);
-                                re[q] = fma(h1.x, s1, re[q]);
-                                re[q] = fma(h2.x, s2, re[q]);
-                                im[q] = fma(h1.y, s1, im[q]);
-                                im[q] = fma(h2.y, s2, im[q]);
+                                const double s1 = SbR[dd].x, s2 = SaR[dc].x;
+                                reB = fma(h1.x, s1, reB);
+                                reB = fma(h2.x, s2, reB);
+                                imB = fma(h1.y, s1, imB);
+                                imB = fma(h2.y, s2, imB);
                             }
-                            if (live[q]) {
-                                F.Hidx[oH + ev[q]] = (int64_t)jv[q] + 1;
-                                F.Hdat[oH + ev[q]] = make_double2(re[q], im[q]);
+                        }
+                        if (leqx) {
+                            if (supxA) {
+                                const int dc = ndA - n_a, dd = ncA - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = flip_sign(SbR[dd].x, sgn_bit), s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                reA = fma(h1.x, s1, reA);
+                                reA = fma(h2.x, s2, reA);
+                                imA = fma(h1.y, s1, imA);
+                                imA = fma(h2.y, s2, imA);
                             }
+                            if (supxB) {
+                                const int dc = ndB - n_a, dd = ncB - n_b;
+                                const double2 h1 = HaR[dc], h2 = HbR[dd];
+                                const double s1 = flip_sign(SbR[dd].x, sgn_bit), s2 = flip_sign(SaR[dc].x, sgn_bit);
+                                reB = fma(h1.x, s1, reB);
+                                reB = fma(h2.x, s2, reB);
+                                imB = fma(h1.y, s1, imB);
+                                imB = fma(h2.y, s2, imB);
+                            }
+                        }
+                        if (liveA) {
+                            F.Hidx[oH + eA] = (int64_t)jA + 1;
+                            F.Hdat[oH + eA] = make_double2(reA, imA);
+                        }
+                        if (liveB) {
+                            F.Hidx[oH + eB] = (int64_t)jB + 1;
+                            F.Hdat[oH + eB] = make_double2(reB, imB);
                         }
                     }
                 } else if (MIXED && BIG && F.s_real && !F.gated && !wide) {
@@ -1175,7 +1181,7 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, con
 // order 9 with k <= 20 stages 48.5 KB), compiled for 4 CTAs per SM so the
 // entry loops get up to 128 registers instead of spilling at 64.
 template <bool MIXED, bool BIG>
-__global__ void __launch_bounds__(128, BIG ? BS2E_FILL_MIN_BLOCKS_BIG : (MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64)) k_csr_fill(FillArgs F) {
+__global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64)) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
     __shared__ int sexp[kMaxK1];

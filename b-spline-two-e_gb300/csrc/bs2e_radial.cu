@@ -261,44 +261,62 @@ __global__ void k_totals(RadialDev P) {
 // 2k FMAs per element instead of up to k^2 products.  Both sums add
 // positive moments (B-splines are non-negative), so the regrouping keeps full
 // accuracy.  Staged per multipole in s[4][k][W]: Pm, SM over dc; m, M over dd;
-// multipoles [g0, g0 + gn) at once, multipole g0 + i at s + i * 4kW.
+// multipoles [g0, g0 + gn) at once, multipole g0 + i at s + i * 4kW.  One
+// thread per (multipole, dc) builds Pm[.][dc] as a running sum over ascending
+// iv1 (each j adds the intervals iv2_j newly passes) and another SM[.][dc]
+// from the top down, so the (a, c) moments are read and added once each.
 __device__ void rk_near_stage(const RadialDev &P, int a, int b, int g0, int gn, double *sg) {
     const int k = P.k, K1 = P.K1, N = P.N, n_iv = P.n_iv, W = 2 * k - 1, k2 = k * k;
-    const int base2 = b - k + 2, per = 2 * W * k;
+    const int base2 = b - k + 2, per = 4 * W * k;
     const double *__restrict__ mom = P.mom;
-    for (int xg = threadIdx.x; xg < gn * per; xg += blockDim.x) {
-        const int gi = xg / per, x = xg - gi * per, kk = g0 + gi;
-        double *s = sg + (size_t)gi * 2 * per;
-        const bool ac = x < W * k;
-        const int y = ac ? x : x - W * k;
+    // (a, c) part: prefix (x even) and suffix (x odd) walkers
+    for (int x = threadIdx.x; x < gn * 2 * W; x += blockDim.x) {
+        const int gi = x / (2 * W), r = x - gi * 2 * W, off = r >> 1, kk = g0 + gi;
+        const bool suf = r & 1;
+        double *s = sg + (size_t)gi * per + (suf ? k * W : 0) + off;  // s[j * W]
+        const int c = a + off - (k - 1);
+        int lop = 0, hip = -1;
+        if (c >= 0 && c < N) {
+            lop = max(max(a, c) - k + 2, 0);
+            hip = min(min(a, c) + 1, n_iv - 1);
+        }
+        const double *mk = mom + (size_t)kk * 2 * k2 + (suf ? k2 : 0) + (a + 1) * k + (c + 1);
+        // moment of interval iv: mk[iv * (K1 2 k^2) - iv * (k + 1)]
+        const size_t ivs = (size_t)K1 * 2 * k2 - (k + 1);
+        double v = 0.0;
+        if (!suf) {
+            int iv1 = lop;
+            for (int j = 0; j < k; ++j) {
+                for (const int lim = min(hip, base2 + j - 1); iv1 <= lim; ++iv1) v += mk[iv1 * ivs];
+                s[j * W] = v;  // Pm: sum over iv1 < iv2_j
+            }
+        } else {
+            int iv1 = hip;
+            for (int j = k - 1; j >= 0; --j) {
+                for (const int lim = max(lop, base2 + j + 1); iv1 >= lim; --iv1) v += mk[iv1 * ivs];
+                s[j * W] = v;  // SM: sum over iv1 > iv2_j
+            }
+        }
+    }
+    // (b, d) part: the moments of the (b, d) pair on iv2_j
+    for (int xg = threadIdx.x; xg < gn * W * k; xg += blockDim.x) {
+        const int gi = xg / (W * k), y = xg - gi * W * k, kk = g0 + gi;
+        double *s = sg + (size_t)gi * per;
         const int off = y / k, j = y - off * k;
         const int iv2 = base2 + j;
         double v0 = 0.0, v1 = 0.0;
-        if (ac) {
-            const int c = a + off - (k - 1);
-            if (c >= 0 && c < N) {
-                const int lop = max(max(a, c) - k + 2, 0), hip = min(min(a, c) + 1, n_iv - 1);
-                for (int iv1 = lop; iv1 <= min(hip, iv2 - 1); ++iv1)
-                    v0 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
-                for (int iv1 = max(lop, iv2 + 1); iv1 <= hip; ++iv1)
-                    v1 += mom[((size_t)iv1 * K1 + kk) * 2 * k2 + k2 + (a + 1 - iv1) * k + (c + 1 - iv1)];
+        const int d = b + off - (k - 1);
+        if (d >= 0 && d < N) {
+            const int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
+            if (iv2 >= loq && iv2 <= hiq) {
+                const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
+                const int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
+                v0 = m2[pb];
+                v1 = m2[k2 + pb];
             }
-            s[j * W + off] = v0;          // Pm
-            s[(k + j) * W + off] = v1;    // SM
-        } else {
-            const int d = b + off - (k - 1);
-            if (d >= 0 && d < N) {
-                const int loq = max(max(b, d) - k + 2, 0), hiq = min(min(b, d) + 1, n_iv - 1);
-                if (iv2 >= loq && iv2 <= hiq) {
-                    const double *m2 = mom + ((size_t)iv2 * K1 + kk) * 2 * k2;
-                    const int pb = (b + 1 - iv2) * k + (d + 1 - iv2);
-                    v0 = m2[pb];
-                    v1 = m2[k2 + pb];
-                }
-            }
-            s[(2 * k + j) * W + off] = v0;  // m(bd)
-            s[(3 * k + j) * W + off] = v1;  // M(bd)
         }
+        s[(2 * k + j) * W + off] = v0;  // m(bd)
+        s[(3 * k + j) * W + off] = v1;  // M(bd)
     }
 }
 
@@ -400,20 +418,21 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
         __syncthreads();  // the previous group's elements are done with s
         rk_near_stage(P, a, b, g0, gn, s);
         __syncthreads();
-        // the group's elements taken in the order (dd, multipole, dc), so the
-        // lanes of a warp mostly share dd: both loops of rk_near_element run
-        // over intervals of the (b, d) pair, and with d common their trip
+        // the group's elements taken in the order (dd, dc, multipole), so the
+        // lanes of a warp share dd and span few dc: both loops of
+        // rk_near_element run over intervals of the (b, d) pair (the second
+        // also of the (a, c) pair), and with d common and c close their trip
         // counts agree across the warp instead of every lane waiting for the
-        // longest (the stores go out W apart, on these few tiles only)
-        const int GW = gn * W, tdd = S / GW, tgi = (S - tdd * GW) / W;
-        const int tdc = S - tdd * GW - tgi * W;
-        int e = threadIdx.x, dd = e / GW, gi = (e - dd * GW) / W, dc = e - dd * GW - gi * W;
+        // longest (the stores go out W^2 apart, on these few tiles only)
+        const int GW = gn * W, tdd = S / GW, tdc = (S - tdd * GW) / gn;
+        const int tgi = S - tdd * GW - tdc * gn;
+        int e = threadIdx.x, dd = e / GW, dc = (e - dd * GW) / gn, gi = e - dd * GW - dc * gn;
         for (; e < gn * W2; e += S) {
             out[(size_t)(g0 + gi) * W2 + dc * W + dd] =
                 rk_near_element(P, s + (size_t)gi * per, a, b, g0 + gi, dc, dd);
-            dd += tdd; gi += tgi; dc += tdc;
-            if (dc >= W) { dc -= W; ++gi; }
-            if (gi >= gn) { gi -= gn; ++dd; }
+            dd += tdd; dc += tdc; gi += tgi;
+            if (gi >= gn) { gi -= gn; ++dc; }
+            if (dc >= W) { dc -= W; ++dd; }
         }
     }
 }
