@@ -364,6 +364,7 @@ __host__ __device__ __forceinline__ size_t rk_scratch(int k, int K1) {
 // out[kk * W^2 + dc * W + dd] (block-wide; s: rk_scratch doubles).  Each
 // thread takes the elements blockDim apart from its own and walks them with an
 // incremental (kk, dc, dd), so no element pays an integer division.
+template <int INTQ>
 __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k_count,
                                double *out, double *s) {
     const int k = P.k, K1 = P.K1, N = P.N, W = 2 * k - 1, W2 = W * W;
@@ -389,13 +390,13 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
         __syncthreads();
         // every thread walks elements e = kk W^2 + dc W + dd, blockDim apart,
         // with an incremental (kk, dc, dd); one product per stored element,
-        // odd warps on the integer pipes (bit for bit the FP64 multiply;
-        // bs2e_dmul.h says why) and even warps on the FP64 pipe, so the two
-        // pipes share the products
+        // INTQ of every four warps on the integer pipes (bit for bit the FP64
+        // multiply; bs2e_dmul.h says why) and the others on the FP64 pipe, so
+        // the two pipes share the products
         const int e1 = (k_first + k_count) * W2;
         int e = k_first * W2 + threadIdx.x;
         int kk = e / W2, dc = (e - kk * W2) / W, dd = e - kk * W2 - dc * W;
-        if ((threadIdx.x >> 5) & 1) {
+        if (((threadIdx.x >> 5) & 3) < INTQ) {
             for (; e < e1; e += S) {
                 out[e] = dmul_int(sx[kk * W + dc], sy[kk * W + dd]);
                 kk += sk; dc += sdc; dd += sdd;
@@ -438,20 +439,22 @@ __device__ void rk_tile_values(const RadialDev &P, int64_t t, int k_first, int k
 }
 
 // Tile t = a * N + b of the FP64 store (block-wide).
+template <int INTQ>
 __device__ void rk_tile_fp64(const RadialDev &P, int64_t t, int k_first, int k_count, double *s) {
     const int k = P.k, K1 = P.K1, W = 2 * k - 1;
     double *dst = P.R + (size_t)t * P.tile;
     const int nel = K1 * W * W;
     for (int e = nel + threadIdx.x; e < P.tile; e += blockDim.x) dst[e] = 0.0;
-    rk_tile_values(P, t, k_first, k_count, dst, s);
+    rk_tile_values<INTQ>(P, t, k_first, k_count, dst, s);
 }
 
 // Tile t of the mixed store (block-wide); sv holds K1 W^2 doubles.
+template <int INTQ>
 __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_count,
                               double *sv, int *sexp, double *s) {
     const int k = P.k, K1 = P.K1, W = 2 * k - 1, W2 = W * W;
     const int nel = K1 * W2;
-    rk_tile_values(P, t, k_first, k_count, sv, s);
+    rk_tile_values<INTQ>(P, t, k_first, k_count, sv, s);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int kk = k_first + warp; kk < k_first + k_count; kk += nwarp) {
@@ -483,15 +486,24 @@ __device__ void rk_tile_mixed(const RadialDev &P, int64_t t, int k_first, int k_
     }
 }
 
+// Quarters of the warps whose far-field products run on the integer pipes.
+// Measured (R^k store, FP64, ms) at order 9 N=800 k<=20 / order 9 N=200 /
+// order 7 N=200 and the 64-problem ragged batch: 0/4 -> 10.38 / 1.24 / 0.338
+// / 91.3; 1/4 -> 9.66 / 1.19 / 0.343 / 97.8; 2/4 -> 10.09 / 1.20 / 0.361 /
+// 98.7; 3/4 -> 12.63 / 1.26 / 0.398 / 103.6.  The batched kernel, capped at
+// 64 registers, keeps every product on the FP64 pipe.
+constexpr int kRkIntQuartersSingle = 1;
+constexpr int kRkIntQuartersBatch = 0;
+
 __global__ void k_rk_store(RadialDev P, int k_first, int k_count) {
     extern __shared__ double scr[];  // rk_scratch(k, K1) doubles
-    rk_tile_fp64(P, blockIdx.x, k_first, k_count, scr);
+    rk_tile_fp64<kRkIntQuartersSingle>(P, blockIdx.x, k_first, k_count, scr);
 }
 
 __global__ void k_rk_store_mixed(RadialDev P, int k_first, int k_count) {
     extern __shared__ double sv[];  // [K1][W][W] FP64 values of the tile, then the scratch
     __shared__ int sexp[kMaxK1];
-    rk_tile_mixed(P, blockIdx.x, k_first, k_count, sv, sexp,
+    rk_tile_mixed<kRkIntQuartersSingle>(P, blockIdx.x, k_first, k_count, sv, sexp,
                   sv + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
 }
 
@@ -555,10 +567,10 @@ __device__ __forceinline__ void batch_body(const BatchStage &B) {
                 const int64_t e = li * blockDim.x + threadIdx.x;
                 if (e < totals_count(P)) totals_elem(P, e);
             } else if (STAGE == 3) {
-                rk_tile_fp64(P, li, 0, P.K1, sm);
+                rk_tile_fp64<kRkIntQuartersBatch>(P, li, 0, P.K1, sm);
                 __syncthreads();
             } else {
-                rk_tile_mixed(P, li, 0, P.K1, sm, sexp,
+                rk_tile_mixed<kRkIntQuartersBatch>(P, li, 0, P.K1, sm, sexp,
                               sm + (size_t)P.K1 * (2 * P.k - 1) * (2 * P.k - 1));
                 __syncthreads();
             }
