@@ -118,6 +118,127 @@ __global__ void __launch_bounds__(256) k_csr_mv(int64_t n_rows, int64_t n_cols, 
     }
 }
 
+// y = A x (op 0) with more loads in flight: each lane takes two consecutive
+// entries per step as k_csr_mv does, but a batch of kMvSteps steps issues all
+// its column-pair and value loads (streaming, evict-first: each is read once)
+// before the x gathers, and the gathers before the FMAs.  One vote per batch
+// decides whether the imaginary FMAs run (every entry of the batch then takes
+// them right after its real ones; a real entry adds +-0, which leaves the
+// sums unchanged), so each lane adds its entries' terms in the same order as
+// k_csr_mv<0>.  Measured over the order-7 N=200 singlet H blocks (1.56e9
+// entries, 37.4 GB per product): k_csr_mv<0> 10.95 ms (3.42 TB/s); batches of
+// 2 steps 6.91 ms (5.42 TB/s, 58 registers), 3 steps 7.24 ms (76), 4 steps
+// 8.24 ms (92: fewer resident warps).
+constexpr int kMvSteps = 2;
+
+__device__ __forceinline__ longlong2 ld_stream_ll2(const int64_t *p) {
+    longlong2 v;
+    asm volatile("ld.global.cs.v2.s64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ double2 ld_stream_d2(const double2 *p) {
+    double2 v;
+    asm volatile("ld.global.cs.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p));
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_csr_mv_n(int64_t n_rows, int64_t n_cols, int64_t nnz,
+                                                  const int64_t *__restrict__ ptr,
+                                                  const int64_t *__restrict__ idx,
+                                                  const double2 *__restrict__ A,
+                                                  const double2 *__restrict__ x,
+                                                  double2 *__restrict__ y,
+                                                  int *__restrict__ bad) {
+    const int64_t row = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (row >= n_rows) return;  // warp-uniform
+    const int64_t j0 = ptr[row] - 1, j1 = ptr[row + 1] - 1;
+    if (j0 < 0 || j1 < j0 || j1 > nnz) {
+        if (lane == 0) atomicOr(bad, 1);
+        return;
+    }
+    double re = 0.0, im = 0.0;
+    int64_t jb = j0;
+    if ((reinterpret_cast<uintptr_t>(idx + jb) & 15) && jb < j1) {
+        // a leading entry off the 16-byte boundary, as in k_csr_mv
+        if (lane == 0) {
+            const int64_t c = idx[jb] - 1;
+            if (c < 0 || c >= n_cols) {
+                atomicOr(bad, 2);
+            } else {
+                const double2 a = A[jb], xv = x[c];
+                re = fma(a.x, xv.x, re);
+                im = fma(a.x, xv.y, im);
+                if ((__double_as_longlong(a.y) << 1) != 0) {
+                    re = fma(-a.y, xv.y, re);
+                    im = fma(a.y, xv.x, im);
+                }
+            }
+        }
+        ++jb;
+    }
+    for (int64_t s = jb; s < j1; s += 64 * kMvSteps) {
+        int64_t c[2 * kMvSteps];
+        double2 a[2 * kMvSteps];
+#pragma unroll
+        for (int u = 0; u < kMvSteps; ++u) {
+            const int64_t j = s + 64 * u + 2 * lane;
+            if (j + 1 < j1) {
+                const longlong2 cc = ld_stream_ll2(idx + j);
+                c[2 * u] = cc.x;
+                c[2 * u + 1] = cc.y;
+                a[2 * u] = ld_stream_d2(A + j);
+                a[2 * u + 1] = ld_stream_d2(A + j + 1);
+            } else {
+                c[2 * u] = j < j1 ? idx[j] : 0;  // 0: no entry here
+                a[2 * u] = j < j1 ? A[j] : make_double2(0.0, 0.0);
+                c[2 * u + 1] = 0;
+                a[2 * u + 1] = make_double2(0.0, 0.0);
+            }
+        }
+        double2 xv[2 * kMvSteps];
+        bool cplx = false;
+#pragma unroll
+        for (int q = 0; q < 2 * kMvSteps; ++q) {
+            const int64_t j = s + 64 * (q >> 1) + 2 * lane + (q & 1);
+            const int64_t cq = c[q] - 1;
+            xv[q] = make_double2(0.0, 0.0);
+            if (j < j1) {
+                if (cq < 0 || cq >= n_cols) {
+                    atomicOr(bad, 2);
+                    a[q] = make_double2(0.0, 0.0);
+                } else {
+                    xv[q] = __ldg(x + cq);
+                }
+            }
+            cplx |= (__double_as_longlong(a[q].y) << 1) != 0;
+        }
+        if (__any_sync(0xffffffffu, cplx)) {
+            asm volatile("" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 2 * kMvSteps; ++q) {
+                re = fma(a[q].x, xv[q].x, re);
+                im = fma(a[q].x, xv[q].y, im);
+                re = fma(-a[q].y, xv[q].y, re);
+                im = fma(a[q].y, xv[q].x, im);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 2 * kMvSteps; ++q) {
+                re = fma(a[q].x, xv[q].x, re);
+                im = fma(a[q].x, xv[q].y, im);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        re += __shfl_xor_sync(0xffffffffu, re, o);
+        im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    if (lane == 0) y[row] = make_double2(re, im);
+}
+
 }  // namespace
 
 void launch_csr_mv(bs2e_handle *h, int op, int64_t n_rows, int64_t n_cols, int64_t nnz,
@@ -131,8 +252,8 @@ void launch_csr_mv(bs2e_handle *h, int op, int64_t n_rows, int64_t n_cols, int64
     const int threads = 256, rows_per_block = threads / 32;
     const int64_t blocks = (n_rows + rows_per_block - 1) / rows_per_block;
     if (op == 0)
-        k_csr_mv<0><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
-                                                                 x, y, bad);
+        k_csr_mv_n<<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
+                                                                x, y, bad);
     else if (op == 1)
         k_csr_mv<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
                                                                  x, y, bad);

@@ -44,6 +44,7 @@ python bench.py --workload order7_n200   the medium drop-in size (order 7, N=200
 python bench.py --profile-band B         one band fill of the large form (small
                                          case for ncu captures of k_csr_fill)
 python bench.py --profile-block B        one whole-block fill of the medium size
+                [--profile-mv]           (and one CSR_mv of its H: small case for ncu)
 python bench.py --workload batch         the ragged batch of 64 radial problems
 python bench.py --workload matvec        CSR mat-vec over medium-size H blocks
 """
@@ -1037,6 +1038,14 @@ def profile_block(args):
         h.block_fill_into(cf, L, True, spin, {x: v.data_ptr() for x, v in Hd.items()},
                           {x: v.data_ptr() for x, v in Sd.items()}, on_device=True)
         h.synchronize()
+        if args.profile_mv:
+            # one y = H x of the block just filled (2.7 GB of CSR read)
+            x = torch.randn(n, dtype=torch.complex128, device=dev)
+            y = torch.empty(n, dtype=torch.complex128, device=dev)
+            torch.cuda.synchronize()
+            h.csr_mv_device(0, n, n, ch, Hd["index_ptr"].data_ptr(), Hd["indices"].data_ptr(),
+                            Hd["data"].data_ptr(), x.data_ptr(), y.data_ptr())
+            h.synchronize()
         print(json.dumps({"profile_block": args.profile_block, "L": L, "spin": spin,
                           "rows": int(n), "nnz_H": ch, "nnz_S": cs,
                           "output_bytes": 24 * (ch + cs)}))
@@ -1264,6 +1273,7 @@ def main():
     ap.add_argument("--profile-block", type=int, default=None)
     ap.add_argument("--profile-band", type=int, default=None)
     ap.add_argument("--profile-nb", type=int, default=200)
+    ap.add_argument("--profile-mv", action="store_true")
     ap.add_argument("--workload", default="order9_n800",
                     choices=["order9_n800", "order7_n200", "batch", "matvec"])
     args = ap.parse_args()

@@ -260,3 +260,38 @@ def test_stream_priority_keeps_products(bs2e, oracle):
             h.set_stream_priority(1000)
         h.set_stream_priority(least)
         _check(h.csr_mv(A, x, 0), want, scale)
+
+
+@pytest.mark.gpu
+def test_gpu_mv_long_rows_mixed_batches(bs2e, oracle):
+    """y = A x on rows of 0..1500 entries: rows span many two-step batches,
+    odd lengths start rows off the 16-byte boundary, complex entries sit in
+    some batches only (the rest take the real-only branch), and a bad column
+    deep inside a row is still caught."""
+    rng = np.random.default_rng(31)
+    n, m = 64, 4000
+    ptr, idx, dat = [1], [], []
+    for i in range(n):
+        ln = int(rng.integers(0, 1500)) | (i & 1)  # odd lengths on odd rows
+        cols = np.sort(rng.choice(m, size=ln, replace=False)) + 1
+        vals = rng.standard_normal(ln).astype(np.complex128)
+        if i % 3 == 0 and ln:
+            k = rng.choice(ln, size=max(1, ln // 200), replace=False)
+            vals[k] += 1j * rng.standard_normal(k.size)
+        idx.extend(cols)
+        dat.extend(vals)
+        ptr.append(len(idx) + 1)
+    A = dict(shape=(n, m), nnz=len(idx), index_ptr=np.array(ptr, np.int64),
+             indices=np.array(idx, np.int64), data=np.array(dat, np.complex128))
+    x = rng.standard_normal(m) + 1j * rng.standard_normal(m)
+    want, scale = oracle.csr_mv(0, A["shape"], A["index_ptr"], A["indices"], A["data"], x)
+    c = CASES["ref60"]
+    with bs2e.Bs2e(oracle_reference("ref60")["knots"], c["k"], c["q"], c["max_k"]) as h:
+        _check(h.csr_mv(A, x, 0), want, scale)
+        bad = dict(A)
+        bad["indices"] = A["indices"].copy()
+        row = int(np.argmax(np.diff(A["index_ptr"])))
+        bad["indices"][A["index_ptr"][row] - 1 + 700] = m + 1
+        with pytest.raises(bs2e.Bs2eError, match="column index"):
+            h.csr_mv(bad, x, 0)
+        _check(h.csr_mv(A, x, 0), want, scale)  # still usable
