@@ -25,8 +25,9 @@ e2e   : the same chunks through the C ABI with HOST buffers: configuration
         lists from pinned host memory, every band and slice copied into
         pinned host buffers (bs2e_block_fill_band / bs2e_dip_block_fill with
         host outputs).
-mixed : the same job on the mixed-precision path (BS2E_PREC_MIXED), its time
-        and its error against the FP64 path on sampled bands.
+mixed : the same job on the mixed-precision path (BS2E_PREC_MIXED), its time,
+        and the errors of both paths against the oracle (and of mixed against
+        FP64) on rows sampled across the blocks.
 roofline: the band fill (k_csr_fill), timed with CUDA events on the
         library's stream; algorithmic bytes = 24 B per stored H/S entry + the
         band's 1-based pointers + the R^k tiles it stages; traffic = DRAM
