@@ -69,56 +69,127 @@ __device__ __forceinline__ void col_sets(const BlockArgs &A, int c_r, int c_c, i
 }
 
 // ---------------------------------------------------------------------------
-// Count: one thread per row.  cnt_H / cnt_S use the construct predicate; the
-// totals of the count_nnz predicate (hamiltonian.f90:386-413) are accumulated
-// in ref[0..1] so the host can detect a block where the two disagree.
+// Count.  cnt_H / cnt_S use the construct predicate; the totals of the
+// count_nnz predicate (hamiltonian.f90:386-413) are accumulated in stats[1..2]
+// (construct totals in stats[3..4]) so the host can detect a block where the
+// two disagree.
 // ---------------------------------------------------------------------------
-__global__ void k_csr_count(BlockArgs A, int64_t *__restrict__ cntH, int64_t *__restrict__ cntS,
-                            unsigned long long *__restrict__ stats) {
-    int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    long long refH = 0, refS = 0, totH = 0, totS = 0;
-    if (row < A.n_rows) {
-        const bs2e_config cf = A.cfg[row];
-        int n_a = (int)cf.n1, n_b = (int)cf.n2;
-        int c_r = A.lmap[cf.l1 * kMaxL + cf.l2];
-        const int k = A.k;
-        int64_t ch = 0, cs = 0;
-        for (int c_c = A.full ? 0 : c_r; c_c < A.n_ch; ++c_c) {
-            int flags = A.pairs[(size_t)c_r * A.n_ch + c_c].flags;
-            bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
-            int nlo = (!A.full && c_c == c_r) ? n_a : 1;
-            Iv2 cand = nc_candidates(n_a, n_b, k, A.N, true, true, nlo);
-            int ncand = cand.l1 + cand.l2;
-            for (int t = 0; t < ncand; ++t) {
-                int n_c = iv2_at(cand, t);
-                Iv2 hs, ss;
-                int base, lo;
-                col_sets(A, c_r, c_c, n_a, n_b, n_c, flags, hs, ss, base, lo);
-                ch += hs.l1 + hs.l2;
-                cs += ss.l1 + ss.l2;
-                // count_nnz semantics: sup entries count if dir_ok, sup_x-only entries if ex_ok
-                size_t s = (size_t)c_c * A.segS + n_c;
-                int lo2 = A.seg_lo[s], hi = A.seg_hi[s];
-                if (A.seg_base[s] < 0) continue;
-                if (!A.full && c_c == c_r && n_c == n_a) lo2 = max(lo2, n_b);
-                if (hi < lo2) continue;
-                bool in_a = abs(n_c - n_a) < k, in_b = abs(n_c - n_b) < k;
-                int ysup = in_a ? ovl(n_b - k + 1, n_b + k - 1, lo2, hi) : 0;
-                int yx = in_b ? ovl(n_a - k + 1, n_a + k - 1, lo2, hi) : 0;
-                int both = (in_a && in_b) ? max(0, min(min(n_b + k - 1, n_a + k - 1), hi) -
-                                                      max(max(n_b - k + 1, n_a - k + 1), lo2) + 1)
-                                          : 0;
-                int xonly = yx - both;
-                refH += (dir_ok ? ysup : 0) + (ex_ok ? xonly : 0);
-                refS += (leq ? ysup : 0) + (leqx ? xonly : 0);
-            }
-        }
-        cntH[row] = ch;
-        cntS[row] = cs;
-        totH = ch;
-        totS = cs;
+
+// Counts of row (c_r, n_a, n_b) in column channel c_c: construct H and S
+// entries and the count_nnz H and S entries.
+__device__ __forceinline__ void count_pair(const BlockArgs &A, int c_r, int c_c, int n_a, int n_b,
+                                           int64_t &ch, int64_t &cs, long long &refH,
+                                           long long &refS) {
+    const int k = A.k;
+    const int flags = A.pairs[(size_t)c_r * A.n_ch + c_c].flags;
+    const bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
+    const int nlo = (!A.full && c_c == c_r) ? n_a : 1;
+    const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, true, true, nlo);
+    const int ncand = cand.l1 + cand.l2;
+    for (int t = 0; t < ncand; ++t) {
+        const int n_c = iv2_at(cand, t);
+        Iv2 hs, ss;
+        int base, lo;
+        col_sets(A, c_r, c_c, n_a, n_b, n_c, flags, hs, ss, base, lo);
+        ch += hs.l1 + hs.l2;
+        cs += ss.l1 + ss.l2;
+        // count_nnz semantics: sup entries count if dir_ok, sup_x-only entries if ex_ok
+        const size_t s = (size_t)c_c * A.segS + n_c;
+        int lo2 = A.seg_lo[s];
+        const int hi = A.seg_hi[s];
+        if (A.seg_base[s] < 0) continue;
+        if (!A.full && c_c == c_r && n_c == n_a) lo2 = max(lo2, n_b);
+        if (hi < lo2) continue;
+        const bool in_a = abs(n_c - n_a) < k, in_b = abs(n_c - n_b) < k;
+        const int ysup = in_a ? ovl(n_b - k + 1, n_b + k - 1, lo2, hi) : 0;
+        const int yx = in_b ? ovl(n_a - k + 1, n_a + k - 1, lo2, hi) : 0;
+        const int both = (in_a && in_b) ? max(0, min(min(n_b + k - 1, n_a + k - 1), hi) -
+                                                     max(max(n_b - k + 1, n_a - k + 1), lo2) + 1)
+                                        : 0;
+        const int xonly = yx - both;
+        refH += (dir_ok ? ysup : 0) + (ex_ok ? xonly : 0);
+        refS += (leq ? ysup : 0) + (leqx ? xonly : 0);
     }
-    // warp reduction of the totals of both predicates
+}
+
+// One CTA per (n_a, n_b) tile, all rows of the tile at once.  Over column
+// channel c_c a row's sets depend on its own channel only through the pair
+// flags: the H set is A (the direct window [n_b - k + 1, n_b + k - 1], where
+// |n_c - n_a| < k) if Aok, B (the exchange window around n_a, where
+// |n_c - n_b| < k) if Bok, their union if both; the S set likewise with leq
+// and leqx; the count_nnz H count is dir_ok |A| + ex_ok |B \ A| and the S
+// count leq |A| + leqx |B \ A|.  So the tile sums SA = sum |A|, SB = sum |B|
+// and SAB = sum |A u B| over the candidates n_c, once per column channel,
+// give every row's counts (|B \ A| sums to SAB - SA) -- exactly the numbers
+// the per-row loop of count_pair adds up, at a few percent of its work (the
+// tile's 20-60 rows share the sums).  Without `full`, a row's own channel
+// takes only n_c >= n_a and its upper triangle, so that pair runs
+// count_pair.
+__global__ void __launch_bounds__(128) k_csr_count_tiles(BlockArgs A, int a0,
+                                                         int64_t *__restrict__ cntH,
+                                                         int64_t *__restrict__ cntS,
+                                                         unsigned long long *__restrict__ stats) {
+    __shared__ int sSA[kMaxCh], sSB[kMaxCh], sSAB[kMaxCh];
+    __shared__ int srow[kMaxCh], sch[kMaxCh], snrow;
+    const int k = A.k;
+    const int n_a = a0 + (int)(blockIdx.x / A.N), n_b = blockIdx.x % A.N + 1;
+    if (threadIdx.x == 0) snrow = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < A.n_ch; c += blockDim.x) {
+        const size_t s = (size_t)c * A.segS + n_a;
+        const int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
+        if (base >= 0 && lo <= n_b && n_b <= hi) {
+            const int slot = atomicAdd(&snrow, 1);
+            srow[slot] = base + (n_b - lo);
+            sch[slot] = c;
+        }
+    }
+    __syncthreads();
+    const int nrow = snrow;
+    if (nrow == 0) return;
+    const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, true, true, 1);
+    const int ncand = cand.l1 + cand.l2;
+    for (int c_c = threadIdx.x; c_c < A.n_ch; c_c += blockDim.x) {
+        int sa = 0, sb = 0, sab = 0;
+        for (int t = 0; t < ncand; ++t) {
+            const int n_c = iv2_at(cand, t);
+            const size_t s = (size_t)c_c * A.segS + n_c;
+            const int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
+            if (base < 0 || hi < lo) continue;
+            const bool in_a = abs(n_c - n_a) < k, in_b = abs(n_c - n_b) < k;
+            const int x10 = max(n_b - k + 1, lo), x11 = min(n_b + k - 1, hi);
+            const int x20 = max(n_a - k + 1, lo), x21 = min(n_a + k - 1, hi);
+            const Iv2 u = make_union(x10, x11, in_a, x20, x21, in_b);
+            sa += in_a ? max(0, x11 - x10 + 1) : 0;
+            sb += in_b ? max(0, x21 - x20 + 1) : 0;
+            sab += u.l1 + u.l2;
+        }
+        sSA[c_c] = sa;
+        sSB[c_c] = sb;
+        sSAB[c_c] = sab;
+    }
+    __syncthreads();
+    long long refH = 0, refS = 0, totH = 0, totS = 0;
+    for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+        const int c_r = sch[r];
+        int64_t ch = 0, cs = 0;
+        const PairInfo *pr = A.pairs + (size_t)c_r * A.n_ch;
+        for (int c_c = A.full ? 0 : c_r + 1; c_c < A.n_ch; ++c_c) {
+            const int flags = pr[c_c].flags;
+            const bool dir_ok = flags & 1, ex_ok = flags & 2, leq = flags & 4, leqx = flags & 8;
+            const bool Aok = dir_ok || leq || leqx, Bok = ex_ok || leq || leqx;
+            const int sa = sSA[c_c], sb = sSB[c_c], sab = sSAB[c_c];
+            ch += Aok ? (Bok ? sab : sa) : (Bok ? sb : 0);
+            cs += leq ? (leqx ? sab : sa) : (leqx ? sb : 0);
+            refH += (dir_ok ? sa : 0) + (ex_ok ? sab - sa : 0);
+            refS += (leq ? sa : 0) + (leqx ? sab - sa : 0);
+        }
+        if (!A.full) count_pair(A, c_r, c_r, n_a, n_b, ch, cs, refH, refS);
+        cntH[srow[r]] = ch;
+        cntS[srow[r]] = cs;
+        totH += ch;
+        totS += cs;
+    }
     for (int o = 16; o > 0; o >>= 1) {
         refH += __shfl_down_sync(0xffffffffu, refH, o);
         refS += __shfl_down_sync(0xffffffffu, refS, o);
@@ -1391,8 +1462,9 @@ void launch_block_count(bs2e_handle *h) {
     A.cfg = h->blk.cfg_new;
     int64_t n = h->plan.n_config;
     if (n > 0) {
-        k_csr_count<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(A, h->blk.cntH, h->blk.cntS,
-                                                                     h->blk.stats);
+        const unsigned tiles = (unsigned)((int64_t)A.N * A.N);
+        k_csr_count_tiles<<<tiles, 128, 0, h->stream>>>(A, 1, h->blk.cntH, h->blk.cntS,
+                                                         h->blk.stats);
         h->launches++;
     }
 }
