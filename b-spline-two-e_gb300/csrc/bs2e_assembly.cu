@@ -365,6 +365,7 @@ struct FillArgs {
     int64_t row0, row1, ptr_row0, Hbase, Sbase;
     const int *band;
     int64_t band_rows;  // rows of the band (pointer slots 0..band_rows)
+    int ch0, ch1;       // only rows of channels [ch0, ch1) are filled
     int a0;  // tile (n_a, n_b) of CTA x: n_a = a0 + x / N, n_b = x % N + 1
     int64_t *Hidx, *Sidx;
     double2 *Hdat, *Sdat;
@@ -1269,7 +1270,7 @@ __global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS :
     // srow keeps each row's output index (its pointer slot)
     if (threadIdx.x == 0) snrow = 0;
     __syncthreads();
-    for (int c = threadIdx.x; c < A.n_ch; c += blockDim.x) {
+    for (int c = F.ch0 + threadIdx.x; c < F.ch1; c += blockDim.x) {
         size_t s = (size_t)c * A.segS + n_a;
         int base = A.seg_base[s], lo = A.seg_lo[s], hi = A.seg_hi[s];
         const int64_t row = base + (n_b - lo);
@@ -1518,6 +1519,8 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
     F.a0 = r.a0;
     F.band = r.band;
     F.band_rows = r.band_rows;
+    F.ch0 = std::max(r.ch0, 0);
+    F.ch1 = r.ch1 < 0 ? F.B.n_ch : std::min(r.ch1, F.B.n_ch);
     size_t smem = fill_smem(h->g);
     if (h->plan.n_config > 0 && r.row1 > r.row0 && r.rows_mode) {
         const unsigned grid = (unsigned)((r.row1 - r.row0 + 3) / 4);

@@ -610,6 +610,7 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_band);
         dfree(h->d_band_idx);
         dfree(h->d_band_val);
+        dfree(h->d_bptr);
         dfree(h->d_stage[0]);
         dfree(h->d_stage[1]);
         if (h->copy_stream) cudaStreamSynchronize(h->copy_stream), cudaStreamDestroy(h->copy_stream);
@@ -960,6 +961,18 @@ static bs2e_status range_ptrs(bs2e_handle *h, int64_t r0, int64_t n) {
     return BS2E_OK;
 }
 
+// The copy stream and the two (filled, copied) event pairs of the staged
+// host-output fills.
+static bs2e_status ensure_copy_stream(bs2e_handle *h) {
+    if (h->copy_stream) return BS2E_OK;
+    CU(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        CU(cudaEventCreateWithFlags(&h->ev_filled[b], cudaEventDisableTiming));
+        CU(cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming));
+    }
+    return BS2E_OK;
+}
+
 // Fills rows [r0, r0 + n) of the counted block into HOST arrays (range-local
 // 1-based index_ptr): the range is cut into chunks that fit one of two
 // staging areas in HBM; the fill of chunk c runs on the handle's stream while
@@ -974,13 +987,7 @@ static bs2e_status stream_fill(bs2e_handle *h, const bs2e_config *cf, int64_t r0
     CU(cudaStreamSynchronize(h->stream));
     const int64_t nH = Hp[n] - 1, nS = Sp[n] - 1;
     if (nH == 0 && nS == 0) return sync_check(h, "block fill");
-    if (!h->copy_stream) {
-        CU(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
-        for (int b = 0; b < 2; ++b) {
-            CU(cudaEventCreateWithFlags(&h->ev_filled[b], cudaEventDisableTiming));
-            CU(cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming));
-        }
-    }
+    TRY(ensure_copy_stream(h));
     // staging areas: the whole range if it fits, else the handle's limit
     // (8 GiB by default; a row holds at most 2 W^2 entries per column channel)
     const int64_t total = 24 * (nH + nS) + 64;
@@ -1384,47 +1391,60 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
     if (!H_index_ptr || !S_index_ptr || (nH > 0 && (!H_indices || !H_data)) ||
         (nS > 0 && (!S_indices || !S_data)))
         return fail(h, BS2E_ERR_ARG, "NULL output array");
-    // device arrays the kernels write: the caller's, or places in a staging area
     const bool dev = out_on_device != 0;
-    int64_t *dHp = H_index_ptr, *dSp = S_index_ptr, *dRows = rows_out, *dHi = H_indices,
-            *dSi = S_indices;
-    double2 *dHd = (double2 *)H_data, *dSd = (double2 *)S_data;
     if (dev) {
         if (!aligned(H_index_ptr, 8) || !aligned(S_index_ptr, 8) || !aligned(H_indices, 8) ||
             !aligned(S_indices, 8) || !aligned(H_data, 16) || !aligned(S_data, 16) ||
             !aligned(rows_out, 8))
             return fail(h, BS2E_ERR_ARG,
                         "device outputs: int64 arrays need 8-byte, data 16-byte alignment");
-    } else {
-        int64_t off = 0;
-        auto take = [&](int64_t bytes) {
-            const int64_t o = off;
-            off += (bytes + 255) / 256 * 256;
-            return o;
-        };
-        const int64_t oHp = take(8 * (nr + 1)), oSp = take(8 * (nr + 1)),
-                      oR = take(rows_out ? 8 * nr : 0), oHi = take(8 * nH), oSi = take(8 * nS),
-                      oHd = take(16 * nH), oSd = take(16 * nS);
-        if (off > h->stage_limit)
-            return fail(h, BS2E_ERR_ARG, "band fill into host arrays: the band needs " +
-                                             std::to_string(off) +
-                                             " bytes, more than a staging area; choose a "
-                                             "narrower band or raise bs2e_opts.stage_bytes");
-        TRY(ensure_stage(h, off));
-        unsigned char *b = h->d_stage[0];
-        dHp = (int64_t *)(b + oHp);
-        dSp = (int64_t *)(b + oSp);
-        dRows = rows_out ? (int64_t *)(b + oR) : nullptr;
-        dHi = (int64_t *)(b + oHi);
-        dSi = (int64_t *)(b + oSi);
-        dHd = (double2 *)(b + oHd);
-        dSd = (double2 *)(b + oSd);
+    }
+    // host outputs: the band is cut into groups of whole channels (a band's
+    // rows, and so its entries, are channel-major, so a group is one slice of
+    // each output array); each group is filled into one of the two staging
+    // areas while the copy stream moves the previous group to the host
+    auto group_bytes = [&](int c0, int c1) {
+        const int64_t hC = boff[c1] - boff[c0], sC = boff[n_ch + 1 + c1] - boff[n_ch + 1 + c0];
+        return (8 * hC + 15) / 16 * 16 + 16 * hC + (8 * sC + 15) / 16 * 16 + 16 * sC;
+    };
+    std::vector<int> cut{0};
+    if (!dev) {
+        const int64_t total = group_bytes(0, n_ch);
+        const int64_t target = std::min<int64_t>(
+            h->stage_limit, std::max<int64_t>(total / 4, (int64_t)64 << 20));
+        while (cut.back() < n_ch) {
+            const int c0 = cut.back();
+            int c1 = c0 + 1;
+            if (group_bytes(c0, c1) > h->stage_limit)
+                return fail(h, BS2E_ERR_ARG,
+                            "band fill into host arrays: channel " + std::to_string(c0) +
+                                " of the band needs " + std::to_string(group_bytes(c0, c1)) +
+                                " bytes, more than a staging area; choose a narrower band or "
+                                "raise bs2e_opts.stage_bytes");
+            while (c1 < n_ch && group_bytes(c0, c1 + 1) <= target) ++c1;
+            cut.push_back(c1);
+        }
     }
     if (!h->d_band) CU(dalloc(&h->d_band, (size_t)2 * kMaxCh));
     if (!h->d_band_val) {
         CU(dalloc(&h->d_band_idx, (size_t)2 * (kMaxCh + 1)));
         CU(dalloc(&h->d_band_val, (size_t)2 * (kMaxCh + 1)));
         h->band_cap = 2 * (kMaxCh + 1);
+    }
+    // band pointers (and rows): the caller's arrays, or the handle's buffer
+    int64_t *dHp = H_index_ptr, *dSp = S_index_ptr, *dRows = rows_out;
+    if (!dev) {
+        const int64_t need = 2 * (nr + 1) + (rows_out ? nr : 0);
+        if (need > h->bptr_cap) {
+            CU(cudaStreamSynchronize(h->stream));
+            dfree(h->d_bptr);
+            h->bptr_cap = 0;
+            CU(dalloc(&h->d_bptr, (size_t)need));
+            h->bptr_cap = need;
+        }
+        dHp = h->d_bptr;
+        dSp = h->d_bptr + nr + 1;
+        dRows = rows_out ? h->d_bptr + 2 * (nr + 1) : nullptr;
     }
     CU(cudaMemcpyAsync(h->d_band, band.data(), sizeof(int) * 2 * n_ch, cudaMemcpyHostToDevice,
                        h->stream));
@@ -1433,30 +1453,89 @@ BS2E_API bs2e_status bs2e_block_fill_band(bs2e_handle *h, const bs2e_config *con
     launch_band_ptr(h, h->d_band, h->d_band_val, n_ch, nr, dHp, dSp, dRows);
     const int64_t a0 = std::max<int64_t>(n1_first, 1),
                   a1 = std::min<int64_t>(n1_first + n1_count - 1, h->g.N);
-    if (nr > 0 && a1 >= a0) {
-        FillRange r;
-        r.row0 = 0;
-        r.row1 = n_config;
-        r.a0 = (int)a0;
-        r.a1 = (int)a1;
-        r.band = h->d_band;
-        r.band_rows = nr;
-        launch_block_fill(h, r, dHp, dSp, dHi, dHd, dSi, dSd);
+    FillRange r;
+    r.row0 = 0;
+    r.row1 = n_config;
+    r.a0 = (int)a0;
+    r.a1 = (int)a1;
+    r.band = h->d_band;
+    r.band_rows = nr;
+    const bool any = nr > 0 && a1 >= a0;
+    if (dev) {
+        if (any) launch_block_fill(h, r, dHp, dSp, H_indices, (double2 *)H_data, S_indices,
+                                   (double2 *)S_data);
+        CU(cudaGetLastError());
+        return sync_check(h, "block fill (band)");
     }
-    CU(cudaGetLastError());
-    if (!dev) {
-        auto d2h = [&](void *dst, const void *src, int64_t bytes) {
-            return bytes > 0 ? cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost,
-                                               h->stream)
-                             : cudaSuccess;
-        };
-        CU(d2h(H_index_ptr, dHp, 8 * (nr + 1)));
-        CU(d2h(S_index_ptr, dSp, 8 * (nr + 1)));
-        if (rows_out) CU(d2h(rows_out, dRows, 8 * nr));
-        CU(d2h(H_indices, dHi, 8 * nH));
-        CU(d2h(S_indices, dSi, 8 * nS));
-        CU(d2h(H_data, dHd, 16 * nH));
-        CU(d2h(S_data, dSd, 16 * nS));
+    const int n_group = (int)cut.size() - 1;
+    int64_t most = 256;
+    for (int g = 0; g < n_group; ++g) most = std::max(most, group_bytes(cut[g], cut[g + 1]));
+    TRY(ensure_stage(h, most));
+    TRY(ensure_copy_stream(h));
+    struct Lay {
+        size_t oHd, oSi, oSd;
+        int64_t h0, hC, s0, sC;
+    };
+    auto lay = [&](int g) {
+        Lay Ly;
+        const int c0 = cut[g], c1 = cut[g + 1];
+        Ly.h0 = boff[c0];
+        Ly.hC = boff[c1] - boff[c0];
+        Ly.s0 = boff[n_ch + 1 + c0];
+        Ly.sC = boff[n_ch + 1 + c1] - Ly.s0;
+        Ly.oHd = (size_t)((8 * Ly.hC + 15) / 16 * 16);
+        Ly.oSi = Ly.oHd + 16 * (size_t)Ly.hC;
+        Ly.oSd = Ly.oSi + (size_t)((8 * Ly.sC + 15) / 16 * 16);
+        return Ly;
+    };
+    cudaError_t e = cudaSuccess;
+    // fill of group g into area g % 2, after the copies out of that area
+    // (group g - 2) are done
+    auto fill = [&](int g) {
+        const int b = g & 1;
+        const Lay Ly = lay(g);
+        unsigned char *base = h->d_stage[b];
+        if (e == cudaSuccess && g >= 2) e = cudaStreamWaitEvent(h->stream, h->ev_copied[b], 0);
+        FillRange rg = r;
+        rg.Hbase = Ly.h0;
+        rg.Sbase = Ly.s0;
+        rg.ch0 = cut[g];
+        rg.ch1 = cut[g + 1];
+        if (e == cudaSuccess && any && (Ly.hC > 0 || Ly.sC > 0)) {
+            launch_block_fill(h, rg, dHp, dSp, (int64_t *)base, (double2 *)(base + Ly.oHd),
+                              (int64_t *)(base + Ly.oSi), (double2 *)(base + Ly.oSd));
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(h->ev_filled[b], h->stream);
+    };
+    auto cp = [&](cudaStream_t st, void *dst, const void *src, size_t bytes) {
+        if (e == cudaSuccess && bytes)
+            e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st);
+    };
+    // the fill of group g + 1 is queued before the copies of group g are
+    // issued: a copy to pageable memory may block the host until it is done
+    if (n_group > 0) fill(0);
+    for (int g = 0; g < n_group && e == cudaSuccess; ++g) {
+        if (g + 1 < n_group) fill(g + 1);
+        const int b = g & 1;
+        const Lay Ly = lay(g);
+        const unsigned char *base = h->d_stage[b];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->copy_stream, h->ev_filled[b], 0);
+        cp(h->copy_stream, H_indices + Ly.h0, base, 8 * (size_t)Ly.hC);
+        cp(h->copy_stream, H_data + 2 * Ly.h0, base + Ly.oHd, 16 * (size_t)Ly.hC);
+        cp(h->copy_stream, S_indices + Ly.s0, base + Ly.oSi, 8 * (size_t)Ly.sC);
+        cp(h->copy_stream, S_data + 2 * Ly.s0, base + Ly.oSd, 16 * (size_t)Ly.sC);
+        if (e == cudaSuccess) e = cudaEventRecord(h->ev_copied[b], h->copy_stream);
+    }
+    cp(h->stream, H_index_ptr, dHp, 8 * (size_t)(nr + 1));
+    cp(h->stream, S_index_ptr, dSp, 8 * (size_t)(nr + 1));
+    if (rows_out) cp(h->stream, rows_out, dRows, 8 * (size_t)nr);
+    cudaError_t e2 = cudaStreamSynchronize(h->copy_stream);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(h->stream);
+        return fail(h, e == cudaErrorMemoryAllocation ? BS2E_ERR_NOMEM : BS2E_ERR_CUDA,
+                    std::string("block fill (band, streamed): ") + cudaGetErrorString(e));
     }
     return sync_check(h, "block fill (band)");
 }

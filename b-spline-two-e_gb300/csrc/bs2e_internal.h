@@ -159,6 +159,8 @@ struct bs2e_handle {
     int *d_band = nullptr;
     int64_t *d_band_idx = nullptr, *d_band_val = nullptr;
     int64_t band_cap = 0;
+    int64_t *d_bptr = nullptr;  // band pointers (H, S, rows) of host-output band fills
+    int64_t bptr_cap = 0;
     // radial dipole bands (M1, M2) and dipole-block work buffers
     double2 *d_dM1 = nullptr, *d_dM2 = nullptr;
     int dip_gauge = -1;
@@ -281,6 +283,7 @@ struct FillRange {
     bool rows_mode = false;
     const int *band = nullptr;
     int64_t band_rows = 0;  // rows of the band when band is set
+    int ch0 = 0, ch1 = -1;  // only rows of channels [ch0, ch1) (ch1 < 0: all)
 };
 // out[i] = src[idx[i]] for i < n (device arrays)
 void launch_gather_i64(bs2e_handle *h, const int64_t *src, const int64_t *idx, int64_t n,

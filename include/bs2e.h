@@ -328,11 +328,14 @@ BS2E_API bs2e_status bs2e_block_fill_rows(bs2e_handle *h, const bs2e_config *con
  * the block's 1-based column indices) and, when rows != NULL (n_rows
  * entries), the 1-based block row of every band row.  out_on_device = 1: the
  * seven arrays are device arrays on the handle's device; 0: host arrays, the
- * band assembled in one of the handle's HBM staging areas
- * (bs2e_opts.stage_bytes) and copied out, so the band must fit one area
- * (BS2E_ERR_ARG otherwise: choose a narrower band).  The same configuration
- * list, L, spin and full as bs2e_block_count_ex.  No counterpart in the
- * reference (its blocks are built whole, hamiltonian.f90:106-283). */
+ * band assembled in groups of whole channels (a band's rows are channel-major,
+ * so a group is one slice of every output array) through the handle's two HBM
+ * staging areas (bs2e_opts.stage_bytes), the copy of one group to the host
+ * running beside the fill of the next; the band's slice of each channel must
+ * fit one area (BS2E_ERR_ARG otherwise: choose a narrower band).  The same
+ * configuration list, L, spin and full as bs2e_block_count_ex.  No
+ * counterpart in the reference (its blocks are built whole,
+ * hamiltonian.f90:106-283). */
 BS2E_API bs2e_status bs2e_block_band_count(bs2e_handle *h, const bs2e_config *configs,
                                            int64_t n_config, int64_t L, int64_t spin,
                                            int64_t full, int64_t n1_first, int64_t n1_count,

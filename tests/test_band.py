@@ -108,6 +108,8 @@ def test_block_cache_off_recounts(bs2e):
 
 
 def test_host_band_larger_than_staging_is_refused(bs2e):
+    """A band whose slice of one channel exceeds a staging area is refused
+    with a message that names the staging area; narrower bands still fill."""
     c = CASES["small2"]
     with bs2e.Bs2e(knots(bs2e, "small2"), c["k"], c["q"], c["max_k"], stage_bytes=65536) as h:
         h.slater()
@@ -119,3 +121,42 @@ def test_host_band_larger_than_staging_is_refused(bs2e):
         assert e.value.status == 1 and "staging" in str(e.value)
         rows, H, S = h.band(cf, L, 1, 1, True, spin)  # one n1 of the first channel fits
         assert rows.size == int((cf["n1"] == 1).sum())
+
+
+def test_host_band_in_channel_groups_equals_device_band(bs2e):
+    """A band larger than one staging area, filled into host arrays in groups
+    of whole channels through the two staging areas (fill of one group beside
+    the copy of the previous), equals the device-output band bit for bit."""
+    torch = pytest.importorskip("torch")
+    c = CASES["small2"]
+    ref = oracle_reference("small2")
+    bl = blocks(bs2e, "small2")
+    L, M, par, spin, cf = max(bl, key=lambda b: b[4].size)
+    with bs2e.Bs2e(knots(bs2e, "small2"), c["k"], c["q"], c["max_k"]) as hd:
+        hd.slater()
+        hd.rk()
+        hd.set_one_body(ref["H1p"], ref["S"])
+        Hd, Sd, rows_d, (r, nh, ns) = _dev_band(torch, hd, cf, L, spin, 1, c["n_b"])
+    total = 40 * (nh + ns)
+    done = False
+    for div in (6, 4, 3, 2):
+        stage = max(total // div, 4096)
+        with bs2e.Bs2e(knots(bs2e, "small2"), c["k"], c["q"], c["max_k"],
+                       stage_bytes=stage) as h:
+            h.slater()
+            h.rk()
+            h.set_one_body(ref["H1p"], ref["S"])
+            try:
+                rows, H, S = h.band(cf, L, 1, c["n_b"], True, spin)
+            except bs2e.Bs2eError as e:
+                assert "staging" in str(e)
+                continue
+        assert stage < 24 * (nh + ns)  # so the band took several groups
+        for A, B in ((H, Hd), (S, Sd)):
+            for key in ("index_ptr", "indices"):
+                np.testing.assert_array_equal(A[key], B[key])
+            np.testing.assert_array_equal(A["data"].view(np.int64), B["data"].view(np.int64))
+        np.testing.assert_array_equal(rows, rows_d)
+        done = True
+        break
+    assert done, "no staging size between a sixth and half of the band worked"
