@@ -559,6 +559,7 @@ BS2E_API bs2e_status bs2e_create(const double *knots, int64_t n_knots, int64_t k
     bad(dalloc(&h->d_tab_Bi, niv * q * q * kk));
     bad(dalloc(&h->d_mom, niv * K1 * 2 * kk * kk));
     bad(dalloc(&h->d_dint, niv * K1 * kk * kk * kk * kk));
+    bad(dalloc(&h->d_dsym, niv * K1 * kk * kk * kk * kk));
     bad(dalloc(&h->d_tot, (size_t)2 * K1 * g.N * g.W));
     bad(dalloc(&h->d_err, 1));
     bad(dalloc(&h->d_range, 4));
@@ -628,6 +629,7 @@ BS2E_API bs2e_status bs2e_destroy(bs2e_handle *h) {
         dfree(h->d_tab_Bi);
         dfree(h->d_mom);
         dfree(h->d_dint);
+        dfree(h->d_dsym);
         dfree(h->d_tot);
         dfree(h->d_R);
         dfree(h->d_Rf);

@@ -9,6 +9,7 @@
 //   tab_Bi  [n_iv][q][q][k]     spline values at the inner radii
 //   mom     [n_iv][K1][2][k][k] per-interval moments (0: int B B r^k, 1: int B B r^-(k+1))
 //   dint    [n_iv][K1][k*k][k*k] same-interval 2-D integrals D(p=(i,i'), q=(j,j'))
+//   dsym    [n_iv][K1][k*k][k*k] D(p, q) + D(q, p), the pair the R^k store adds
 //   tot     [2][K1][N][W]       moments summed over all shared intervals of a pair
 //   R       [N][N][tile]        R^k store, tile = [K1][W][W] padded to 16 bytes:
 //                               R^k[a,b,c,d] at tile(a,b)[k][c-a+k-1][d-b+k-1]
@@ -134,7 +135,7 @@ struct bs2e_handle {
     double *d_tab_D1 = nullptr;  // first derivatives (velocity-gauge dipoles)
     double *d_tab_r = nullptr, *d_tab_B = nullptr, *d_tab_D2 = nullptr, *d_tab_ri = nullptr,
            *d_tab_Bi = nullptr;
-    double *d_mom = nullptr, *d_dint = nullptr, *d_tot = nullptr;
+    double *d_mom = nullptr, *d_dint = nullptr, *d_dsym = nullptr, *d_tot = nullptr;
     double *d_R = nullptr;      // FP64 store
     float2 *d_Rf = nullptr;     // mixed store: scaled (hi, lo) pairs, same tile layout
     int32_t *d_Rexp = nullptr;  // mixed store: power-of-two scale per (tile, k)
@@ -210,7 +211,7 @@ cudaError_t noalloc_prepare(int device, bool refresh);
 struct RadialDev {
     const double *knots, *glx, *glw;
     double *tab_r, *tab_B, *tab_D2, *tab_D1, *tab_ri, *tab_Bi;
-    double *mom, *dint, *tot, *R;
+    double *mom, *dint, *dsym, *tot, *R;
     float2 *Rf;
     int *Rexp;
     int k, q, K1, N, n_iv, mixed;

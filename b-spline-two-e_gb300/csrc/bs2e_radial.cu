@@ -193,6 +193,22 @@ __device__ void moments_item(const RadialDev &Pd, int iv, int kk, double *sm) {
             ++p;
         }
     }
+    // the symmetric sums D(p, q) + D(q, p) the R^k store adds per shared
+    // interval, formed once here (the same additions, so the store is the
+    // same bit for bit); the barrier makes the CTA's D writes visible
+    __syncthreads();
+    double *__restrict__ dsym = Pd.dsym;
+    p = threadIdx.x / k2;
+    qq = threadIdx.x - p * k2;
+    for (int e = threadIdx.x; e < k2 * k2; e += blockDim.x) {
+        dsym[dbase + e] = dint[dbase + e] + dint[dbase + (size_t)qq * k2 + p];
+        p += step_p;
+        qq += step_q;
+        if (qq >= k2) {
+            qq -= k2;
+            ++p;
+        }
+    }
 }
 
 __global__ void k_moments(RadialDev P) {
@@ -338,8 +354,8 @@ __device__ __forceinline__ double rk_near_element(const RadialDev &P, const doub
     const int hi = min(min(min(a, c), min(b, d)) + 1, n_iv - 1);
     for (int iv = lo; iv <= hi; ++iv) {
         const int pa = (a + 1 - iv) * k + (c + 1 - iv), pb = (b + 1 - iv) * k + (d + 1 - iv);
-        const double *D = P.dint + ((size_t)iv * K1 + kk) * (size_t)k2 * k2;
-        v += D[(size_t)pa * k2 + pb] + D[(size_t)pb * k2 + pa];
+        // D(iv; ac, bd) + D(iv; bd, ac), summed once by the moments stage
+        v += P.dsym[((size_t)iv * K1 + kk) * (size_t)k2 * k2 + (size_t)pa * k2 + pb];
     }
     return v;
 }
@@ -765,6 +781,7 @@ RadialDev radial_dev(const bs2e_handle *h) {
     P.tab_Bi = h->d_tab_Bi;
     P.mom = h->d_mom;
     P.dint = h->d_dint;
+    P.dsym = h->d_dsym;
     P.tot = h->d_tot;
     P.R = h->d_R;
     P.Rf = h->d_Rf;
