@@ -143,6 +143,10 @@ __device__ __forceinline__ double2 ld_stream_d2(const double2 *p) {
     return v;
 }
 
+// SYM: CSR_mv_sym with the same loads: entries below the diagonal are
+// dropped, the row's sum is added to y (zeroed) atomically, and every entry
+// above the diagonal adds a x(row) to y(column) as in k_csr_mv<2>.
+template <bool SYM>
 __global__ void __launch_bounds__(256) k_csr_mv_n(int64_t n_rows, int64_t n_cols, int64_t nnz,
                                                   const int64_t *__restrict__ ptr,
                                                   const int64_t *__restrict__ idx,
@@ -166,13 +170,21 @@ __global__ void __launch_bounds__(256) k_csr_mv_n(int64_t n_rows, int64_t n_cols
             const int64_t c = idx[jb] - 1;
             if (c < 0 || c >= n_cols) {
                 atomicOr(bad, 2);
-            } else {
+            } else if (!SYM || c >= row) {
                 const double2 a = A[jb], xv = x[c];
                 re = fma(a.x, xv.x, re);
                 im = fma(a.x, xv.y, im);
                 if ((__double_as_longlong(a.y) << 1) != 0) {
                     re = fma(-a.y, xv.y, re);
                     im = fma(a.y, xv.x, im);
+                }
+                if (SYM && c > row) {
+                    const double2 xr = x[row];
+                    double tr = fma(a.x, xr.x, 0.0), ti = fma(a.x, xr.y, 0.0);
+                    tr = fma(-a.y, xr.y, tr);
+                    ti = fma(a.y, xr.x, ti);
+                    atomicAdd(&y[c].x, tr);
+                    atomicAdd(&y[c].y, ti);
                 }
             }
         }
@@ -208,9 +220,14 @@ __global__ void __launch_bounds__(256) k_csr_mv_n(int64_t n_rows, int64_t n_cols
                 if (cq < 0 || cq >= n_cols) {
                     atomicOr(bad, 2);
                     a[q] = make_double2(0.0, 0.0);
+                } else if (SYM && cq < row) {
+                    a[q] = make_double2(0.0, 0.0);  // below the diagonal: not read
+                    c[q] = 0;
                 } else {
                     xv[q] = __ldg(x + cq);
                 }
+            } else {
+                c[q] = 0;
             }
             cplx |= (__double_as_longlong(a[q].y) << 1) != 0;
         }
@@ -230,13 +247,35 @@ __global__ void __launch_bounds__(256) k_csr_mv_n(int64_t n_rows, int64_t n_cols
                 im = fma(a[q].x, xv[q].y, im);
             }
         }
+        if (SYM) {
+            // the mirrored half: a x(row) into y(column) for columns past the row
+            const double2 xr = x[row];
+#pragma unroll
+            for (int q = 0; q < 2 * kMvSteps; ++q) {
+                const int64_t cq = c[q] - 1;
+                if (cq > row && cq < n_cols) {
+                    double tr = fma(a[q].x, xr.x, 0.0), ti = fma(a[q].x, xr.y, 0.0);
+                    tr = fma(-a[q].y, xr.y, tr);
+                    ti = fma(a[q].y, xr.x, ti);
+                    atomicAdd(&y[cq].x, tr);
+                    atomicAdd(&y[cq].y, ti);
+                }
+            }
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         re += __shfl_xor_sync(0xffffffffu, re, o);
         im += __shfl_xor_sync(0xffffffffu, im, o);
     }
-    if (lane == 0) y[row] = make_double2(re, im);
+    if (lane == 0) {
+        if (SYM) {
+            atomicAdd(&y[row].x, re);
+            atomicAdd(&y[row].y, im);
+        } else {
+            y[row] = make_double2(re, im);
+        }
+    }
 }
 
 }  // namespace
@@ -252,14 +291,14 @@ void launch_csr_mv(bs2e_handle *h, int op, int64_t n_rows, int64_t n_cols, int64
     const int threads = 256, rows_per_block = threads / 32;
     const int64_t blocks = (n_rows + rows_per_block - 1) / rows_per_block;
     if (op == 0)
-        k_csr_mv_n<<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
-                                                                x, y, bad);
+        k_csr_mv_n<false><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr,
+                                                                       idx, A, x, y, bad);
     else if (op == 1)
         k_csr_mv<1><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
                                                                  x, y, bad);
     else
-        k_csr_mv<2><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr, idx, A,
-                                                                 x, y, bad);
+        k_csr_mv_n<true><<<(unsigned)blocks, threads, 0, h->stream>>>(n_rows, n_cols, nnz, ptr,
+                                                                      idx, A, x, y, bad);
     h->launches++;
 }
 
