@@ -286,6 +286,7 @@ class Bs2e:
         self.knots = np.ascontiguousarray(knots, dtype=np.float64)
         self.k, self.k_GL, self.max_k = int(k), int(k_GL), int(max_k)
         self.K1 = self.max_k + 1
+        self.precision = int(precision)
         opts = _Opts()
         L_.bs2e_default_opts(ctypes.byref(opts))
         opts.precision = int(precision)
