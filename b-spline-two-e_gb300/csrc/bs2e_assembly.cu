@@ -381,13 +381,13 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
 // banded one-body lookup M[x][y] (1-based), zero outside the band
 __device__ __forceinline__ double2 band(const double2 *M, int N, int k, int x, int y) {
     int d = y - x;
-    if (d >= k || -d >= k) return make_double2(0.0, 0.0);
+    if (abs(d) >= k) return make_double2(0.0, 0.0);
     return M[(size_t)(x - 1) * (2 * k - 1) + (d + k - 1)];
 }
 
 __device__ __forceinline__ float4 bandf(const float4 *M, int k, int x, int y) {
     int d = y - x;
-    if (d >= k || -d >= k) return make_float4(0.f, 0.f, 0.f, 0.f);
+    if (abs(d) >= k) return make_float4(0.f, 0.f, 0.f, 0.f);
     return M[(size_t)(x - 1) * (2 * k - 1) + (d + k - 1)];
 }
 

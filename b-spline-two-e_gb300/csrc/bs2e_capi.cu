@@ -1587,6 +1587,7 @@ BS2E_API bs2e_status bs2e_radial_dipole(bs2e_handle *h, int64_t gauge, double *r
     launch_radial_dip(h, (int)gauge);
     TRY(sync_check(h, "radial dipole"));
     h->dip_gauge = (int)gauge;
+    h->dip_kind = gauge == 0 ? 1 : 2;  // <r> is real, -i<d/dr> and -i<1/r> imaginary
     double *outs[2] = {gauge == 0 ? r_mat : dr_mat, gauge == 1 ? r_inv_mat : nullptr};
     double2 *src[2] = {h->d_dM1, h->d_dM2};
     for (int m = 0; m < 2; ++m) {
@@ -1617,6 +1618,7 @@ BS2E_API bs2e_status bs2e_set_radial_dipole(bs2e_handle *h, int64_t gauge, const
     dfree(h->d_dM1);
     dfree(h->d_dM2);
     double2 **dst[2] = {&h->d_dM1, &h->d_dM2};
+    bool all_re = true, all_im = true;  // every band value real / imaginary
     for (int m = 0; m < 2; ++m) {
         if (!ins[m]) continue;
         std::vector<double2> b((size_t)N * W, make_double2(0.0, 0.0));
@@ -1626,11 +1628,14 @@ BS2E_API bs2e_status bs2e_set_radial_dipole(bs2e_handle *h, int64_t gauge, const
                 if (y < 0 || y >= N) continue;
                 size_t o = ((size_t)y * N + x) * 2;
                 b[(size_t)x * W + d] = make_double2(ins[m][o], ins[m][o + 1]);
+                all_re = all_re && ins[m][o + 1] == 0.0;
+                all_im = all_im && ins[m][o] == 0.0;
             }
         CU(dalloc(dst[m], b.size()));
         CU(cudaMemcpy(*dst[m], b.data(), b.size() * sizeof(double2), cudaMemcpyHostToDevice));
     }
     h->dip_gauge = (int)gauge;
+    h->dip_kind = all_re ? 1 : (all_im ? 2 : 0);
     return BS2E_OK;
 }
 

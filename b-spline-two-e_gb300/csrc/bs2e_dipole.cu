@@ -25,7 +25,7 @@ namespace {
 
 __device__ __forceinline__ double2 bnd(const double2 *M, int k, int x, int y) {
     int d = y - x;
-    if (M == nullptr || d >= k || -d >= k) return make_double2(0.0, 0.0);
+    if (M == nullptr || abs(d) >= k) return make_double2(0.0, 0.0);
     return M[(size_t)(x - 1) * (2 * k - 1) + (d + k - 1)];
 }
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
@@ -86,8 +86,32 @@ __global__ void k_dip_count(DipArgs A, int64_t *__restrict__ cnt,
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&stats[3], (unsigned long long)tot);
 }
 
+// The entry value in real arithmetic when S and the radial dipole bands are
+// real (P = 0: the value is real) or S real and the bands imaginary (P = 1:
+// the value is imaginary, the imaginary parts carry it): one product-sum per
+// term instead of a complex one.
+template <int P>
+__device__ __forceinline__ double dterm_part(double a, double b, const double *M1, const double *M2,
+                                             const double *S, int k, int x, int y, int u, int v,
+                                             double acc) {
+    if (a == 0.0 && b == 0.0) return acc;
+    const int W = 2 * k - 1;
+    const int d = y - x, e = v - u;
+    // (written with abs: the equivalent test `d >= k || -d >= k || e >= k ||
+    // -e >= k` came out wrong for some inputs in this function on sm_103a,
+    // checked against a CPU reference over all (x, y, u, v) of a 24-spline
+    // grid; the abs form and an unsigned range test were exact)
+    if (abs(d) >= k || abs(e) >= k) return acc;
+    const size_t om = (size_t)(x - 1) * W + (d + k - 1), os = (size_t)(u - 1) * W + (e + k - 1);
+    const double m = a * M1[2 * om + P] + (M2 ? b * M2[2 * om + P] : 0.0);
+    return fma(m, S[2 * os], acc);
+}
+
 // One warp per row; lanes enumerate the (n_c, n_d) runs of each column channel
-// exactly as the H assembly does, so columns come out ascending.
+// exactly as the H assembly does, so columns come out ascending.  MODE 0:
+// complex arithmetic; 1: S and the dipole bands real; 2: S real, the bands
+// imaginary (the radial dipoles the library computes are one or the other).
+template <int MODE>
 __global__ void __launch_bounds__(128) k_dip_fill(DipArgs A, const int64_t *__restrict__ ptr,
                                                   int64_t *__restrict__ idx,
                                                   double2 *__restrict__ dat) {
@@ -137,13 +161,26 @@ __global__ void __launch_bounds__(128) k_dip_fill(DipArgs A, const int64_t *__re
                 if (e < tot) {
                     const int o = e - o_ex;
                     const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
-                    double2 v = dterm(pp.c[0], pp.c[1], A.M1, A.M2, A.Sb, k, n_a, r_nc, n_b, n_d);
-                    double2 t = dterm(pp.c[2], pp.c[3], A.M1, A.M2, A.Sb, k, n_b, n_d, n_a, r_nc);
-                    v = make_double2(v.x + t.x, v.y + t.y);
-                    t = dterm(pp.c[4], pp.c[5], A.M1, A.M2, A.Sb, k, n_a, n_d, n_b, r_nc);
-                    v = make_double2(v.x + t.x, v.y + t.y);
-                    t = dterm(pp.c[6], pp.c[7], A.M1, A.M2, A.Sb, k, n_b, r_nc, n_a, n_d);
-                    v = make_double2(v.x + t.x, v.y + t.y);
+                    double2 v;
+                    if (MODE == 0) {
+                        v = dterm(pp.c[0], pp.c[1], A.M1, A.M2, A.Sb, k, n_a, r_nc, n_b, n_d);
+                        double2 t = dterm(pp.c[2], pp.c[3], A.M1, A.M2, A.Sb, k, n_b, n_d, n_a, r_nc);
+                        v = make_double2(v.x + t.x, v.y + t.y);
+                        t = dterm(pp.c[4], pp.c[5], A.M1, A.M2, A.Sb, k, n_a, n_d, n_b, r_nc);
+                        v = make_double2(v.x + t.x, v.y + t.y);
+                        t = dterm(pp.c[6], pp.c[7], A.M1, A.M2, A.Sb, k, n_b, r_nc, n_a, n_d);
+                        v = make_double2(v.x + t.x, v.y + t.y);
+                    } else {
+                        constexpr int P = MODE == 1 ? 0 : 1;
+                        const double *M1 = (const double *)A.M1, *M2 = (const double *)A.M2;
+                        const double *S = (const double *)A.Sb;
+                        double s = 0.0;
+                        s = dterm_part<P>(pp.c[0], pp.c[1], M1, M2, S, k, n_a, r_nc, n_b, n_d, s);
+                        s = dterm_part<P>(pp.c[2], pp.c[3], M1, M2, S, k, n_b, n_d, n_a, r_nc, s);
+                        s = dterm_part<P>(pp.c[4], pp.c[5], M1, M2, S, k, n_a, n_d, n_b, r_nc, s);
+                        s = dterm_part<P>(pp.c[6], pp.c[7], M1, M2, S, k, n_b, r_nc, n_a, n_d, s);
+                        v = MODE == 1 ? make_double2(s, 0.0) : make_double2(0.0, s);
+                    }
                     idx[o_row + e] = (int64_t)(r_base + (n_d - r_lo)) + 1;
                     dat[o_row + e] = v;
                 }
@@ -219,7 +256,14 @@ void launch_dip_fill(bs2e_handle *h, const DipDev &D, const int64_t *ptr, int64_
     DipArgs A{D.rows, D.n_rows, D.lmap_r, D.seg, D.seg + D.nseg, D.seg + 2 * D.nseg, h->g.N + 2,
               D.n_ch_r, D.n_ch_c, h->g.N, h->g.k, D.pairs, h->d_dM1, h->d_dM2, h->d_Sb};
     if (D.n_rows > 0) {
-        k_dip_fill<<<(unsigned)((D.n_rows + 3) / 4), 128, 0, h->stream>>>(A, ptr, idx, dat);
+        const unsigned grid = (unsigned)((D.n_rows + 3) / 4);
+        const int mode = h->s_real ? h->dip_kind : 0;
+        if (mode == 1)
+            k_dip_fill<1><<<grid, 128, 0, h->stream>>>(A, ptr, idx, dat);
+        else if (mode == 2)
+            k_dip_fill<2><<<grid, 128, 0, h->stream>>>(A, ptr, idx, dat);
+        else
+            k_dip_fill<0><<<grid, 128, 0, h->stream>>>(A, ptr, idx, dat);
         h->launches++;
     }
 }

@@ -165,6 +165,7 @@ struct bs2e_handle {
     // radial dipole bands (M1, M2) and dipole-block work buffers
     double2 *d_dM1 = nullptr, *d_dM2 = nullptr;
     int dip_gauge = -1;
+    int dip_kind = 0;  // radial dipole bands: 1 all real, 2 all imaginary, 0 general
     bs2e_config *d_dip_rows = nullptr, *d_dip_cols = nullptr;
     int64_t dip_rows_cap = 0, dip_cols_cap = 0;
     int *d_dip_lmap = nullptr, *d_dip_seg = nullptr;

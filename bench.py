@@ -678,6 +678,8 @@ def run_large(args, rank, world):
                               / n_jobs_local,
         "radial_s": sums.get("radial", 0) / max(1, sum(1 for s in range(args.steps) if s % nc == 0)),
         "consume_s_per_job": sums.get("consume", 0) / n_jobs_local,
+        "stage_s_per_job": {x: sums.get(x, 0) / n_jobs_local
+                            for x in ("count", "fill", "dipole", "consume")},
         "rk_stage_elements_per_s": None,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": "k_csr_fill (band fills)", "achieved": achieved,

@@ -289,3 +289,34 @@ def test_device_radial_dipole_drives_blocks(bs2e, oracle):
     np.testing.assert_array_equal(got["indices"], want["indices"])
     np.testing.assert_allclose(got["data"], want["data"], rtol=0,
                                atol=1e-12 * np.abs(want["data"]).max())
+
+
+def test_dipole_blocks_with_complex_bands_match_oracle(bs2e, oracle):
+    """Radial dipole bands with both real and imaginary parts (a caller's own
+    matrices) take the fill's general complex arithmetic; the library's own
+    bands are real (length gauge) or imaginary (velocity gauge) and take the
+    real-arithmetic forms checked above."""
+    c = CASES["small2"]
+    ref = oracle_reference("small2")
+    mats = oracle.setup_radial_dip(ref["knots"], c["k"], c["q"], 0)
+    r_mat = np.asarray(mats[0]) * (0.8 + 0.6j)
+    mats_c = (r_mat,) + tuple(mats[1:])
+    bl = [b for b in blocks(bs2e, "small2") if b[3] == 0]
+    (L1, M1, p1, _, rows), (L2, M2, p2, _, cols) = bl[0], bl[1]
+    with _handle(bs2e, "small2") as h:
+        h.set_one_body(ref["H1p"], ref["S"])
+        h.set_radial_dipole(0, r_mat=r_mat)
+        n_checked = 0
+        for q in (-1, 0, 1):
+            want = oracle.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), q, True, c["k"],
+                                    c["n_b"], 0, ref["S"], mats_c)
+            got = h.dip_block(rows, (L1, M1, p1), cols, (L2, M2, p2), q, True)
+            assert got["nnz"] == want["nnz"]
+            if want["nnz"] == 0:
+                continue
+            n_checked += 1
+            np.testing.assert_array_equal(got["indices"], want["indices"])
+            scale = np.abs(want["data"]).max()
+            np.testing.assert_allclose(got["data"], want["data"], rtol=0, atol=1e-12 * scale)
+            assert np.abs(got["data"].imag).max() > 0.1 * scale  # the imaginary parts are there
+        assert n_checked > 0
