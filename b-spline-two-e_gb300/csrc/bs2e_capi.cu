@@ -375,6 +375,8 @@ DipPair dip_pair(int L1, int L2, double ang3j, int gauge, int la, int lb, int lc
         p.c[6] = f * al;
         p.c[7] = f * be;
     }
+    for (int t = 0; t < 4; ++t)
+        if (p.c[2 * t] != 0.0 || p.c[2 * t + 1] != 0.0) p.tm |= 1 << t;
     return p;
 }
 

@@ -31,10 +31,10 @@ __device__ __forceinline__ double2 bnd(const double2 *M, int k, int x, int y) {
 __device__ __forceinline__ double2 cmul2(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-// (a M1 + b M2)(x, y) * S(u, v)
+// (a M1 + b M2)(x, y) * S(u, v); the caller skips terms whose a and b are
+// both zero
 __device__ __forceinline__ double2 dterm(double a, double b, const double2 *M1, const double2 *M2,
                                          const double2 *Sb, int k, int x, int y, int u, int v) {
-    if (a == 0.0 && b == 0.0) return make_double2(0.0, 0.0);
     double2 m1 = bnd(M1, k, x, y), m2 = bnd(M2, k, x, y);
     double2 m = make_double2(a * m1.x + b * m2.x, a * m1.y + b * m2.y);
     return cmul2(m, bnd(Sb, k, u, v));
@@ -89,12 +89,12 @@ __global__ void k_dip_count(DipArgs A, int64_t *__restrict__ cnt,
 // The entry value in real arithmetic when S and the radial dipole bands are
 // real (P = 0: the value is real) or S real and the bands imaginary (P = 1:
 // the value is imaginary, the imaginary parts carry it): one product-sum per
-// term instead of a complex one.
+// term instead of a complex one.  The caller skips terms whose a and b are
+// both zero.
 template <int P>
 __device__ __forceinline__ double dterm_part(double a, double b, const double *M1, const double *M2,
                                              const double *S, int k, int x, int y, int u, int v,
                                              double acc) {
-    if (a == 0.0 && b == 0.0) return acc;
     const int W = 2 * k - 1;
     const int d = y - x, e = v - u;
     // (written with abs: the equivalent test `d >= k || -d >= k || e >= k ||
@@ -126,6 +126,12 @@ __global__ void __launch_bounds__(128) k_dip_fill(DipArgs A, const int64_t *__re
     for (int cc = 0; cc < A.n_ch_c; ++cc) {
         const DipPair pp = A.pairs[(size_t)cr * A.n_ch_c + cc];
         if (!pp.ok) continue;
+        // which of the four terms have a non-zero coefficient pair, decided
+        // on the host: a double comparison runs on GB300's FP64 pipe, and the
+        // eight of them per channel pair, on rows of ~50 entries per pair,
+        // kept that pipe 82% busy while the entries' own products used 11%
+        // of it (order-9 N=200 slice of the L=4 -> 5 block, 181e6 entries)
+        const int tm = pp.tm;
         const Iv2 cand = nc_candidates(n_a, n_b, k, A.N, true, true, 1);
         const int ncand = cand.l1 + cand.l2;
         for (int g0 = 0; g0 < ncand; g0 += 32) {
@@ -163,22 +169,23 @@ __global__ void __launch_bounds__(128) k_dip_fill(DipArgs A, const int64_t *__re
                     const int n_d = o < r_l1 ? r_s1 + o : r_s2 + (o - r_l1);
                     double2 v;
                     if (MODE == 0) {
-                        v = dterm(pp.c[0], pp.c[1], A.M1, A.M2, A.Sb, k, n_a, r_nc, n_b, n_d);
-                        double2 t = dterm(pp.c[2], pp.c[3], A.M1, A.M2, A.Sb, k, n_b, n_d, n_a, r_nc);
+                        const double2 z = make_double2(0.0, 0.0);
+                        v = (tm & 1) ? dterm(pp.c[0], pp.c[1], A.M1, A.M2, A.Sb, k, n_a, r_nc, n_b, n_d) : z;
+                        double2 t = (tm & 2) ? dterm(pp.c[2], pp.c[3], A.M1, A.M2, A.Sb, k, n_b, n_d, n_a, r_nc) : z;
                         v = make_double2(v.x + t.x, v.y + t.y);
-                        t = dterm(pp.c[4], pp.c[5], A.M1, A.M2, A.Sb, k, n_a, n_d, n_b, r_nc);
+                        t = (tm & 4) ? dterm(pp.c[4], pp.c[5], A.M1, A.M2, A.Sb, k, n_a, n_d, n_b, r_nc) : z;
                         v = make_double2(v.x + t.x, v.y + t.y);
-                        t = dterm(pp.c[6], pp.c[7], A.M1, A.M2, A.Sb, k, n_b, r_nc, n_a, n_d);
+                        t = (tm & 8) ? dterm(pp.c[6], pp.c[7], A.M1, A.M2, A.Sb, k, n_b, r_nc, n_a, n_d) : z;
                         v = make_double2(v.x + t.x, v.y + t.y);
                     } else {
                         constexpr int P = MODE == 1 ? 0 : 1;
                         const double *M1 = (const double *)A.M1, *M2 = (const double *)A.M2;
                         const double *S = (const double *)A.Sb;
                         double s = 0.0;
-                        s = dterm_part<P>(pp.c[0], pp.c[1], M1, M2, S, k, n_a, r_nc, n_b, n_d, s);
-                        s = dterm_part<P>(pp.c[2], pp.c[3], M1, M2, S, k, n_b, n_d, n_a, r_nc, s);
-                        s = dterm_part<P>(pp.c[4], pp.c[5], M1, M2, S, k, n_a, n_d, n_b, r_nc, s);
-                        s = dterm_part<P>(pp.c[6], pp.c[7], M1, M2, S, k, n_b, r_nc, n_a, n_d, s);
+                        if (tm & 1) s = dterm_part<P>(pp.c[0], pp.c[1], M1, M2, S, k, n_a, r_nc, n_b, n_d, s);
+                        if (tm & 2) s = dterm_part<P>(pp.c[2], pp.c[3], M1, M2, S, k, n_b, n_d, n_a, r_nc, s);
+                        if (tm & 4) s = dterm_part<P>(pp.c[4], pp.c[5], M1, M2, S, k, n_a, n_d, n_b, r_nc, s);
+                        if (tm & 8) s = dterm_part<P>(pp.c[6], pp.c[7], M1, M2, S, k, n_b, r_nc, n_a, n_d, s);
                         v = MODE == 1 ? make_double2(s, 0.0) : make_double2(0.0, s);
                     }
                     idx[o_row + e] = (int64_t)(r_base + (n_d - r_lo)) + 1;

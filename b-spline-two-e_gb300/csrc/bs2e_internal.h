@@ -98,7 +98,8 @@ struct DevBlock {
 // (alpha, beta) coefficients of the four one-particle terms, with the 3j
 // factor, the 6j/sqrt factors and the exchange phase folded in.
 struct DipPair {
-    int32_t ok, pad;
+    int32_t ok;
+    int32_t tm;  // bit t: term t has a non-zero coefficient pair c[2t], c[2t+1]
     double c[8];
 };
 

@@ -10,9 +10,12 @@ and the assembly of the 6 symmetry blocks (5.3e11 H and S entries) and the
 5 dipole blocks (~6e10 entries): ~14 TB of CSR, more than HBM and host memory
 together.  The CSR is therefore made in n1 bands (bs2e_block_fill_band) and
 dipole row slices of at most one staging area (24 GiB; two areas in turn)
-and consumed on the device as it is made: the mat-vec bs2e_csr_mv applies
-every band of H and S and every slice of D to a fixed vector (the product a
-solver needs), on a second handle's stream while the next band fills.
+and consumed on the device as it is made, on a second stream while the next
+band fills: the mat-vec bs2e_csr_mv applies every band of H and S and every
+slice of D to a fixed vector (the product a solver needs), or with
+--consume digest a 64-bit wrapping sum of every word of every band and slice
+(pointers, columns and the bit patterns of the values) reads them instead.
+Either way a chunk made again must give the same sum.
 
 A bench step is 1/16 of a job: the job's bands and slices cut into 16
 chunks of nearly equal CSR bytes, chunk 0 also running the radial stage, so
@@ -46,6 +49,8 @@ python bench.py --workload order7_n200   the medium drop-in size (order 7, N=200
                                          triplet), whole blocks into HBM
 python bench.py --profile-band B         one band fill of the large form (small
                                          case for ncu captures of k_csr_fill)
+python bench.py --profile-dip B          one dipole row slice (block B -> B+1) of the
+                                         large form's method (small case for k_dip_fill)
 python bench.py --profile-block B        one whole-block fill of the medium size
                 [--profile-mv]           (and one CSR_mv of its H: small case for ncu)
 python bench.py --workload batch         the ragged batch of 64 radial problems
@@ -294,18 +299,21 @@ class LargeJob:
     chunks; run_chunk(j) assembles chunk j into the two staging areas and
     applies it to fixed vectors with the library's mat-vec."""
 
-    def __init__(self, pkg, w, prec, areas, rank=0, world=1, plan=None):
+    def __init__(self, pkg, w, prec, areas, rank=0, world=1, plan=None, consume="mv"):
         import torch
         self.torch = torch
         self.pkg, self.w = pkg, w
+        self.consume = consume
+        self.digests = {}  # chunk -> [device sum of each run: int64 digest or complex y sum]
         self.dev = torch.device("cuda", torch.cuda.current_device())
         t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
         self.h = pkg.Bs2e(t, w["k"], w["q"], w["max_k"], precision=prec,
                           device=self.dev.index, stage_bytes=w["area_bytes"])
         self.h.set_block_cache(0)
         self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
-        # the consumer: a second handle (any basis; it only runs the mat-vec on
-        # device pointers) whose stream works while the next band fills, at
+        # the consumer: a second handle (any basis; it only lends its stream
+        # to the digest sums, or runs the mat-vec on device pointers) whose
+        # stream works while the next band fills, at
         # the highest stream priority so its CTAs take SM slots as fill CTAs
         # retire instead of waiting for the whole band
         self.hc = pkg.Bs2e(pkg.grids.explin_knots(6, 24, 20.0), 6, 8, 0, device=self.dev.index)
@@ -431,8 +439,9 @@ class LargeJob:
     def run_chunk(self, j, timers=None):
         """Chunk j on the device; timers: dict of lists of (event, event) pairs.
         Units fill the two areas in turn on the library's stream; a consumer
-        thread applies each filled unit on the consumer handle's stream while
-        the next unit fills; the call returns when both are done."""
+        thread digests (or applies) each filled unit on the consumer handle's
+        stream while the next unit fills; the call returns when both are
+        done."""
         import queue
         import threading
         torch, h = self.torch, self.h
@@ -456,6 +465,10 @@ class LargeJob:
         for f in free:
             f.set()
         err = []
+        with torch.cuda.stream(self.cstream):
+            digest = torch.zeros((), dtype=torch.int64 if self.consume == "digest" else
+                                 torch.complex128, device=self.dev)
+        self.digests.setdefault(j, []).append(digest)
 
         def consumer():
             try:
@@ -466,10 +479,17 @@ class LargeJob:
                     a, n_rows, n_cols, mats, x = item
                     e0 = start(self.cstream)
                     for (nnz, P, I, D) in mats:
-                        self.hc.csr_mv_device(0, n_rows, n_cols, nnz, P, I, D, x,
-                                              self.y.data_ptr())
-                        self._acc(n_rows)
+                        if self.consume == "mv":
+                            self.hc.csr_mv_device(0, n_rows, n_cols, nnz, P, I, D, x,
+                                                  self.y.data_ptr())
+                            self._acc(n_rows, digest)
+                        else:
+                            with torch.cuda.stream(self.cstream):
+                                for ptr, n in ((P, n_rows + 1), (I, nnz), (D, 2 * nnz)):
+                                    digest.add_(self._words(a, ptr, n).sum())
                     mark("consume", e0, self.cstream)
+                    if self.consume != "mv":
+                        self.cstream.synchronize()
                     free[a].set()
             except BaseException as e:  # the producer re-raises it
                 err.append(e)
@@ -524,9 +544,25 @@ class LargeJob:
         if err:
             raise err[0]
 
-    def _acc(self, r):
+    def _acc(self, r, chunk_sum):
         with self.torch.cuda.stream(self.cstream):
-            self.ysum += self.y[:r].sum()
+            s = self.y[:r].sum()
+            self.ysum += s
+            chunk_sum += s
+
+    def _words(self, a, ptr, n):
+        """The n 64-bit words at device address ptr inside area a."""
+        area = self.areas[a]
+        off = ptr - area.data_ptr()
+        assert off % 8 == 0 and 0 <= off and off + 8 * n <= area.numel() * 8
+        return area.view(self.torch.int64)[off // 8:off // 8 + n]
+
+    def digest_repeats(self):
+        """(chunks made more than once, whether every repeat gave the same
+        sum, bit for bit)."""
+        runs = {j: [d.cpu().numpy().tobytes() for d in v] for j, v in self.digests.items()
+                if len(v) > 1}
+        return len(runs), all(len(set(v)) == 1 for v in runs.values())
 
     def e2e_units(self, h, units, host, counted):
         """Units through the C ABI on handle h with host outputs (pinned buffers
@@ -611,7 +647,7 @@ def run_large(args, rank, world):
              for _ in range(2)]
     prec_main = args.precision
     precs = {"fp64": pkg.PREC_FP64, "mixed": pkg.PREC_MIXED}
-    job = LargeJob(pkg, w, precs[prec_main], areas, rank, world)
+    job = LargeJob(pkg, w, precs[prec_main], areas, rank, world, consume=args.consume)
     nc = w["n_chunks"]
     elems = rk_elements(w)
     total_bytes = sum(u["bytes"] for u in job.plan["units"])
@@ -671,8 +707,11 @@ def run_large(args, rank, world):
                                           for u in job.plan["units"]),
                    "nnz_dipole_per_job": sum(u.get("nnz", 0) for u in job.plan["units"]),
                    "l2": "every step writes ~%.0f GB of CSR (> L2)" % (total_bytes / nc / 1e9),
-                   "consumer": "bs2e_csr_mv of every band of H and S and slice of D with a "
-                               "fixed vector, on the device"},
+                   "consumer": ("bs2e_csr_mv of every band of H and S and slice of D with a "
+                                "fixed vector, on the device" if args.consume == "mv" else
+                                "64-bit wrapping sum of every word of every band of H and S "
+                                "and slice of D (pointers, columns, value bit patterns), on "
+                                "the device")},
         "job_s": job_s, "jobs_timed": jobs_done,
         "assembly_s_per_job": (sums.get("fill", 0) + sums.get("dipole", 0) + sums.get("count", 0))
                               / n_jobs_local,
@@ -689,8 +728,14 @@ def run_large(args, rank, world):
                      "note": "achieved = (24 B per H/S entry + pointers + staged R^k tiles) / "
                              "CUDA-event time of the band-fill calls on the library stream"},
         "clocks": clk.summary(),
-        "checksum_y": complex(job.ysum.item()).__repr__(),
     }
+    n_rep, same = job.digest_repeats()
+    res["repeat_check"] = {"chunks_made_again": n_rep, "sums_repeat_bit_exact": same}
+    if args.consume == "mv":
+        res["checksum_y"] = complex(job.ysum.item()).__repr__()
+    elif all(j in job.digests for j in range(nc)):
+        res["repeat_check"]["job_digest"] = "%016x" % (
+            sum(int(job.digests[j][0].item()) for j in range(nc)) & (2 ** 64 - 1))
     if res["radial_s"]:
         res["rk_stage_elements_per_s"] = elems / res["radial_s"]
     cs = CpuSample(pkg, w) if rank == 0 and world == 1 else None
@@ -698,7 +743,8 @@ def run_large(args, rank, world):
     # both against the oracle on rows of every block
     if not args.no_mixed and world == 1:
         other = "mixed" if prec_main == "fp64" else "fp64"
-        job2 = LargeJob(pkg, w, precs[other], areas, rank, world, plan=job.plan)
+        job2 = LargeJob(pkg, w, precs[other], areas, rank, world, plan=job.plan,
+                        consume=args.consume)
         job2.run_chunk(0)
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
@@ -1062,6 +1108,41 @@ def profile_band(args):
                           8 * tile_doubles(w) * tiles, "tiles": int(tiles)}))
 
 
+def profile_dip(args):
+    """One dipole row slice of the large form's method (order 9, q=12,
+    l_max=10, length gauge) on N = --profile-nb splines (r_max = N): rows of
+    singlet block --profile-dip against block --profile-dip + 1, taken from the
+    middle of the block until ~160e6 entries (~3.9 GB of CSR, above L2): the
+    small case for ncu captures of k_dip_fill."""
+    import torch
+    pkg = _pkg()
+    w = dict(LARGE, n_b=args.profile_nb, r_max=float(args.profile_nb))
+    t = pkg.grids.explin_knots(w["k"], w["n_b"], w["r_max"])
+    blocks = block_list(pkg, w)
+    (L1, M1, p1, _, c1), (L2, M2, p2, _, c2) = blocks[args.profile_dip], blocks[args.profile_dip + 1]
+    with pkg.Bs2e(t, w["k"], w["q"], w["max_k"]) as h:
+        h.slater()
+        h.one_body(w["Z"], w["l_max"] + 1, w["cap_order"], w["cap_r0"], w["cap_eta"],
+                   copy_out=False)
+        h.radial_dipole(0, copy_out=False)
+        s1, s2 = (L1, M1, p1), (L2, M2, p2)
+        per_row = h.dip_block_count(c1, s1, c2, s2, 0) / max(c1.size, 1)
+        n_rows = int(min(c1.size, max(1, 160e6 / max(per_row, 1.0))))
+        r0 = (c1.size - n_rows) // 2
+        rows = c1[r0:r0 + n_rows]
+        n = h.dip_block_count(rows, s1, c2, s2, 0)
+        dev = torch.device("cuda", 0)
+        mk = lambda m, dt: torch.empty(max(int(m), 1), dtype=dt, device=dev)
+        D = dict(index_ptr=mk(n_rows + 1, torch.int64), indices=mk(n, torch.int64),
+                 data=mk(n, torch.complex128))
+        torch.cuda.synchronize()
+        h.dip_block_into(rows, s1, c2, s2, 0, {x: v.data_ptr() for x, v in D.items()})
+        h.synchronize()
+        print(json.dumps({"profile_dip": [args.profile_dip, args.profile_dip + 1],
+                          "L": [L1, L2], "rows": [int(r0), int(r0 + n_rows)], "nnz": int(n),
+                          "algorithmic_bytes": 24 * n + 8 * (n_rows + 1)}))
+
+
 def profile_block(args):
     """Small case for ncu: one radial pass, then count + fill of one block of
     the medium size into device buffers (block 0: 117,620 rows, ~2.9 GB)."""
@@ -1320,10 +1401,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--consume", default="mv", choices=["mv", "digest"])
     ap.add_argument("--profile-block", type=int, default=None)
     ap.add_argument("--profile-band", type=int, default=None)
     ap.add_argument("--profile-nb", type=int, default=200)
     ap.add_argument("--profile-mv", action="store_true")
+    ap.add_argument("--profile-dip", type=int, default=None)
     ap.add_argument("--workload", default="order9_n800",
                     choices=["order9_n800", "order7_n200", "batch", "matvec"])
     args = ap.parse_args()
@@ -1332,6 +1415,9 @@ def main():
         return
     if args.profile_band is not None:
         profile_band(args)
+        return
+    if args.profile_dip is not None:
+        profile_dip(args)
         return
     if args.workload == "batch":
         print(json.dumps(run_batch(args)), flush=True)
