@@ -313,11 +313,11 @@ class LargeJob:
         self.stream = torch.cuda.ExternalStream(self.h.stream, device=self.dev)
         # the consumer: a second handle (any basis; it only lends its stream
         # to the digest sums, or runs the mat-vec on device pointers) whose
-        # stream works while the next band fills, at
-        # the highest stream priority so its CTAs take SM slots as fill CTAs
-        # retire instead of waiting for the whole band
+        # stream works while the next band fills.  Both streams keep the
+        # default priority.  Jobs timed back to back on one GB300 took
+        # 8.74-8.87 s this way, 9.21-9.43 s with the consumer at the highest
+        # priority, and 8.64 or 9.62 s with the fill's stream at the highest.
         self.hc = pkg.Bs2e(pkg.grids.explin_knots(6, 24, 20.0), 6, 8, 0, device=self.dev.index)
-        self.hc.set_stream_priority(torch.cuda.Stream.priority_range()[1])
         self.cstream = torch.cuda.ExternalStream(self.hc.stream, device=self.dev)
         self.areas = areas
         self.blocks = [(L, M, par, spin, self._pin(cf)) for (L, M, par, spin, cf)
@@ -733,7 +733,7 @@ def run_large(args, rank, world):
     res["repeat_check"] = {"chunks_made_again": n_rep, "sums_repeat_bit_exact": same}
     if args.consume == "mv":
         res["checksum_y"] = complex(job.ysum.item()).__repr__()
-    elif all(j in job.digests for j in range(nc)):
+    elif args.consume == "digest" and all(j in job.digests for j in range(nc)):
         res["repeat_check"]["job_digest"] = "%016x" % (
             sum(int(job.digests[j][0].item()) for j in range(nc)) & (2 ** 64 - 1))
     if res["radial_s"]:
