@@ -1254,16 +1254,25 @@ __device__ __forceinline__ void fill_row(const FillArgs &F, const int local, con
 }
 
 // BIG: the variant for R^k tiles too large for 8 CTAs per SM (above ~22 KB:
-// order 9 with k <= 20 stages 48.5 KB), compiled for 4 CTAs per SM so the
-// entry loops get up to 128 registers instead of spilling at 64.
+// order 9 with k <= 20 stages 48.5 KB), compiled for 4 CTAs per SM.  Warps
+// per CTA: the FP64 kernel's loop is bound by FP64 issue, and more warps keep
+// the pipe fed while others find their entries.  Four order-9 N=800 bands
+// (2.1e9 entries) took 19.6 ms with 4 warps (120 registers), 19.2 with 5
+// (96), 18.0-18.6 with 6 (80) and 18.1-18.2 with 7 (72, no spills); 7 is the
+// most whose shared memory fits four CTAs on an SM (four of 48.5 KB tile +
+// 8 KB static + 1 KB reserved).  The mixed kernel needs its 128 registers.
 template <bool MIXED, bool BIG>
-__global__ void __launch_bounds__(128, BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64)) k_csr_fill(FillArgs F) {
+__host__ __device__ constexpr int fill_warps() { return BIG && !MIXED ? 7 : 4; }
+
+template <bool MIXED, bool BIG>
+__global__ void __launch_bounds__(32 * fill_warps<MIXED, BIG>(), BIG ? 4 : (MIXED ? BS2E_FILL_MIN_BLOCKS : BS2E_FILL_MIN_BLOCKS_FP64)) k_csr_fill(FillArgs F) {
     extern __shared__ __align__(128) double sR[];
     __shared__ uint64_t bar;
     __shared__ int sexp[kMaxK1];
-    __shared__ float2 sA[4][2][kMaxK1];
-    __shared__ int sKo[4][2][kMaxK1];
-    __shared__ int srow[kMaxCh], sch[kMaxCh], snrow, snext;
+    __shared__ float2 sA[fill_warps<MIXED, BIG>()][2][kMaxK1];
+    __shared__ int sKo[fill_warps<MIXED, BIG>()][2][kMaxK1];
+    __shared__ int srow[kMaxCh], snrow, snext;
+    __shared__ uint8_t sch[kMaxCh];
     __shared__ int snz[kMaxCh];
     __shared__ uint8_t sord[kMaxCh];
     static_assert(kMaxCh <= 256, "row order kept in bytes");
@@ -1539,15 +1548,15 @@ void launch_block_fill(bs2e_handle *h, const FillRange &r, const int64_t *d_Hptr
         const unsigned tiles = (unsigned)((int64_t)(r.a1 - r.a0 + 1) * h->g.N);
         // 8 CTAs of 128 threads fit an SM while each stages at most ~22 KB
         const bool big = smem > (size_t)22 * 1024;
-        auto go = [&](auto kern) {
+        auto go = [&](auto kern, int threads) {
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            kern<<<tiles, 128, smem, h->stream>>>(F);
+            kern<<<tiles, threads, smem, h->stream>>>(F);
         };
         const bool mixed = h->precision == BS2E_PREC_MIXED;
-        if (mixed && big) go(k_csr_fill<true, true>);
-        else if (mixed) go(k_csr_fill<true, false>);
-        else if (big) go(k_csr_fill<false, true>);
-        else go(k_csr_fill<false, false>);
+        if (mixed && big) go(k_csr_fill<true, true>, 32 * fill_warps<true, true>());
+        else if (mixed) go(k_csr_fill<true, false>, 32 * fill_warps<true, false>());
+        else if (big) go(k_csr_fill<false, true>, 32 * fill_warps<false, true>());
+        else go(k_csr_fill<false, false>, 32 * fill_warps<false, false>());
         h->launches++;
     }
 }
